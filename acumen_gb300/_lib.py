@@ -1,0 +1,99 @@
+"""ctypes binding of libacumen_gpu.so (the C ABI declared in include/acumen_gpu.h).
+
+The shared library is built in-tree by ``acumen_gb300.build.build()``.  There is
+no CPU fallback: if the library is missing, every entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libacumen_gpu.so")
+
+ACU_OK = 0
+ACU_ERR_INVALID = -1
+ACU_ERR_CUDA = -2
+ACU_ERR_NOMEM = -3
+ACU_ERR_TIMEOUT = -4
+ACU_ERR_UNSUPPORTED = -5
+
+ACU_OPT_FILTER = 1
+ACU_OPT_LANES = 2
+ACU_OPT_GRAPH = 3
+ACU_OPT_VERBOSE = 4
+ACU_OPT_PRINT_EVERY = 5
+ACU_OPT_SLICE_BASE = 6
+
+_ERRNAMES = {ACU_ERR_INVALID: "invalid argument", ACU_ERR_CUDA: "CUDA error", ACU_ERR_NOMEM: "out of memory",
+             ACU_ERR_TIMEOUT: "device wait timed out", ACU_ERR_UNSUPPORTED: "unsupported"}
+
+
+class AcumenError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{_ERRNAMES.get(code, 'error')} ({code}): {msg}")
+        self.code = code
+
+
+_lib = None
+P = ctypes.c_void_p
+I = ctypes.c_int
+F = ctypes.c_float
+D = ctypes.c_double
+
+# name -> argument types; every function returns int
+SIGNATURES = {
+    "acu_ctx_create": [ctypes.POINTER(P), I, I, P, I],
+    "acu_ctx_destroy": [P],
+    "acu_set_stream": [P, P],
+    "acu_set_option": [P, I, I],
+    "acu_get_option": [P, I, ctypes.POINTER(I)],
+    "acu_iradon": [P, I, P, P],
+    "acu_radon": [P, I, P, P],
+    "acu_radon_adjoint": [P, I, P, P],
+    "acu_iradon_dev": [P, I, P, P],
+    "acu_radon_dev": [P, I, P, P],
+    "acu_radon_adjoint_dev": [P, I, P, P],
+    "acu_filter_dev": [P, I, P, P],
+    "acu_backproject_dev": [P, I, P, P],
+    "acu_iradon_dev_f64": [P, I, P, P],
+    "acu_radon_dev_f64": [P, I, P, P],
+    "acu_radon_adjoint_dev_f64": [P, I, P, P],
+    "acu_tvopt": [P, I, P, I, I, I, F, F, P, P],
+    "acu_tvopt_dev": [P, I, P, I, I, I, F, F, P, P],
+    "acu_tvopt_plain": [P, I, P, I, I, I, F, F, P, P],
+    "acu_tvopt_plain_dev": [P, I, P, I, I, I, F, F, P, P],
+    "acu_tvopt_dev_f64": [P, I, P, I, I, I, D, D, P, P],
+    "acu_tv_last_delta": [P, I, P],
+}
+
+
+def lib():
+    """Load the library (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"{LIB_PATH} is missing: run acumen_gb300.build.build() (nvcc, sm_103a) first; "
+                               "there is no CPU fallback")
+        L = ctypes.CDLL(LIB_PATH)
+        for name, args in SIGNATURES.items():
+            fn = getattr(L, name, None)
+            if fn is None:
+                continue
+            fn.argtypes = args
+            fn.restype = I
+        L.acu_last_error.argtypes = [P]
+        L.acu_last_error.restype = ctypes.c_char_p
+        _lib = L
+    return _lib
+
+
+def check(rc: int, ctx=None):
+    if rc != ACU_OK:
+        msg = lib().acu_last_error(ctx)
+        raise AcumenError(rc, msg.decode() if msg else "")
+    return rc
+
+
+def call(name: str, *args, ctx=None):
+    return check(getattr(lib(), name)(*args), ctx)

@@ -1,0 +1,707 @@
+// C ABI of libacumen_gpu.so: contexts, the Radon operators and the batched /
+// per-slice split-Bregman TV solvers (tomography/tv_hpc.F90:1-390).
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/acumen_gpu.h"
+#include "kernels.h"
+#include "tables.h"
+
+using namespace acu;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t n = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf&) = delete;
+    DevBuf& operator=(const DevBuf&) = delete;
+    ~DevBuf() { release(); }
+    void release()
+    {
+        if (p) cudaFree(p);
+        p = nullptr;
+        n = 0;
+    }
+    // grow-only; returns a cudaError_t
+    cudaError_t ensure(size_t bytes)
+    {
+        if (bytes <= n && p) return cudaSuccess;
+        release();
+        if (bytes == 0) bytes = 16;
+        cudaError_t e = cudaMalloc(&p, bytes);
+        if (e != cudaSuccess) {
+            p = nullptr;
+            return e;
+        }
+        n = bytes;
+        return cudaSuccess;
+    }
+    template <typename T>
+    T* as() const { return reinterpret_cast<T*>(p); }
+};
+
+template <typename Real>
+struct GeomSet {
+    bool ready = false;
+    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_tw;
+    DevGeom<Real> d;
+};
+
+// Work buffers of the TV solver for one precision (lane layout, G groups).
+template <typename Real>
+struct TvState {
+    DevBuf f, fk, ruk, rp, q;                                   // T*N per slice
+    DevBuf uk, ukp, dx, dy, bx, by, rhs, r, p, Ap, tmp;         // N*N per slice
+    DevBuf rsold, alpha, beta, delta, part;                     // FP64 scalars
+    cudaGraphExec_t graph = nullptr;
+    std::string graph_key;
+    ~TvState()
+    {
+        if (graph) cudaGraphExecDestroy(graph);
+    }
+};
+
+}  // namespace
+
+struct acu_ctx {
+    int N = 0, T = 0, wpu = 0;
+    std::vector<float> theta;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    int opt_filter = 0;  // FFT ramp filter
+    int opt_lanes = 0;
+    int opt_graph = 1;
+    int opt_verbose = 0;
+    int opt_print_every = 50;
+    int opt_slice_base = 1;
+    std::string err;
+    GeomSet<float> g32;
+    GeomSet<double> g64;
+    // operator work buffers
+    DevBuf w_in, w_out, w_q, w_host_in, w_host_out;
+    TvState<float> tv32;
+    TvState<double> tv64;
+    std::vector<double> last_delta;
+};
+
+namespace {
+
+int set_err(acu_ctx* ctx, int code, const char* fmt, ...)
+{
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof buf, fmt, ap);
+    va_end(ap);
+    if (ctx) ctx->err = buf;
+    g_last_error = buf;
+    return code;
+}
+
+#define CK(ctx, call)                                                                           \
+    do {                                                                                        \
+        cudaError_t e_ = (call);                                                                \
+        if (e_ != cudaSuccess)                                                                  \
+            return set_err(ctx, e_ == cudaErrorMemoryAllocation ? ACU_ERR_NOMEM : ACU_ERR_CUDA, \
+                           "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+    } while (0)
+
+#define CKLAUNCH(ctx) CK(ctx, cudaGetLastError())
+
+#define CKRET(expr)              \
+    do {                         \
+        int r_ = (expr);         \
+        if (r_ != ACU_OK) return r_; \
+    } while (0)
+
+template <typename Real>
+GeomSet<Real>& geomset(acu_ctx* c);
+template <>
+GeomSet<float>& geomset<float>(acu_ctx* c) { return c->g32; }
+template <>
+GeomSet<double>& geomset<double>(acu_ctx* c) { return c->g64; }
+
+template <typename Real>
+int ensure_geom(acu_ctx* c)
+{
+    GeomSet<Real>& gs = geomset<Real>(c);
+    if (gs.ready) return ACU_OK;
+    if (c->N <= 0) return set_err(c, ACU_ERR_INVALID, "context has no reconstruction grid (nimage = 0)");
+    HostTables<Real> h;
+    make_tables<Real>(c->N, c->T, c->theta.data(), c->wpu, h);
+    CK(c, gs.sc_bp.ensure(sizeof(Real) * h.sc_bp.size()));
+    CK(c, gs.sc_fp.ensure(sizeof(Real) * h.sc_fp.size()));
+    CK(c, gs.filt.ensure(sizeof(Real) * (h.filt.size() + 8)));
+    CK(c, gs.cmask.ensure(sizeof(Real) * h.cmask.size()));
+    CK(c, gs.fft_h.ensure(sizeof(Real) * h.fft_h.size()));
+    std::vector<float> tw32(h.fft_tw.begin(), h.fft_tw.end());
+    CK(c, gs.fft_tw.ensure(sizeof(double) * h.fft_tw.size()));
+    CK(c, cudaMemcpy(gs.sc_bp.p, h.sc_bp.data(), sizeof(Real) * h.sc_bp.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(gs.sc_fp.p, h.sc_fp.data(), sizeof(Real) * h.sc_fp.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemset(gs.filt.p, 0, sizeof(Real) * (h.filt.size() + 8)));
+    CK(c, cudaMemcpy(gs.filt.p, h.filt.data(), sizeof(Real) * h.filt.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(gs.cmask.p, h.cmask.data(), sizeof(Real) * h.cmask.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(gs.fft_h.p, h.fft_h.data(), sizeof(Real) * h.fft_h.size(), cudaMemcpyHostToDevice));
+    if (sizeof(Real) == 4)
+        CK(c, cudaMemcpy(gs.fft_tw.p, tw32.data(), sizeof(float) * tw32.size(), cudaMemcpyHostToDevice));
+    else
+        CK(c, cudaMemcpy(gs.fft_tw.p, h.fft_tw.data(), sizeof(double) * h.fft_tw.size(), cudaMemcpyHostToDevice));
+    gs.d.N = c->N;
+    gs.d.T = c->T;
+    gs.d.mid = h.mid;
+    gs.d.sc_bp = gs.sc_bp.template as<Real>();
+    gs.d.sc_fp = gs.sc_fp.template as<Real>();
+    gs.d.filt = gs.filt.template as<Real>();
+    gs.d.cmask = gs.cmask.template as<Real>();
+    gs.d.fft_h = gs.fft_h.template as<Real>();
+    gs.d.fft_tw = gs.fft_tw.template as<float2>();
+    gs.d.fft_tw64 = gs.fft_tw.template as<double2>();
+    gs.d.fft_L = h.fft_L;
+    gs.d.fft_log2L = h.fft_log2L;
+    gs.ready = true;
+    return ACU_OK;
+}
+
+int check_ctx(acu_ctx* c, int nslices)
+{
+    if (!c) return set_err(nullptr, ACU_ERR_INVALID, "null context");
+    if (c->N <= 0) return set_err(c, ACU_ERR_INVALID, "context has no reconstruction grid (nimage = 0)");
+    if (nslices < 0) return set_err(c, ACU_ERR_INVALID, "nslices must be >= 0 (got %d)", nslices);
+    return ACU_OK;
+}
+
+// Slices per thread of the batched kernels.
+int pick_lanes(const acu_ctx* c, int S, bool is_double)
+{
+    if (is_double) return 1;
+    if (c->opt_lanes == 1 || c->opt_lanes == 4) return c->opt_lanes;
+    return S >= 4 ? 4 : 1;
+}
+
+// ---- operators in lane layout ---------------------------------------------
+template <typename Real, int V>
+void lanes_filter(acu_ctx* c, const DevGeom<Real>& g, int G, const Real* in, Real* out)
+{
+    if (c->opt_filter == 0 && g.fft_L > 0 && fft_fits<Real>(g.fft_L))
+        launch_filter_fft<Real, V>(g, G, in, out, c->stream);
+    else
+        launch_filter_direct<Real, V>(g, G, in, out, c->stream);
+}
+
+template <typename Real, int V>
+void lanes_iradon(acu_ctx* c, const DevGeom<Real>& g, int G, const Real* sino, Real* q, Real* img)
+{
+    lanes_filter<Real, V>(c, g, G, sino, q);
+    launch_backproject<Real, V>(g, G, q, img, c->stream);
+}
+
+enum OpKind { OP_IRADON, OP_RADON, OP_RADON_ADJ, OP_FILTER, OP_BACKPROJECT };
+
+// Runs one operator on plain-layout device arrays of S slices.
+template <typename Real, int V>
+int run_op_v(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
+{
+    CKRET(ensure_geom<Real>(c));
+    const DevGeom<Real>& g = geomset<Real>(c).d;
+    const int N = c->N, T = c->T;
+    const int G = (S + V - 1) / V;
+    const size_t nsino = (size_t)T * N, nimg = (size_t)N * N;
+    const bool in_sino = (op != OP_RADON);
+    const bool out_sino = (op == OP_RADON || op == OP_FILTER);
+    const size_t nin = in_sino ? nsino : nimg, nout = out_sino ? nsino : nimg;
+    const Real* lin = in;
+    Real* lout = out;
+    if constexpr (V > 1) {
+        CK(c, c->w_in.ensure(sizeof(Real) * nin * G * V));
+        CK(c, c->w_out.ensure(sizeof(Real) * nout * G * V));
+        launch_to_lanes<Real, V>(in, c->w_in.template as<Real>(), S, nin, c->stream);
+        lin = c->w_in.template as<Real>();
+        lout = c->w_out.template as<Real>();
+    }
+    switch (op) {
+    case OP_IRADON:
+        CK(c, c->w_q.ensure(sizeof(Real) * nsino * G * V));
+        lanes_iradon<Real, V>(c, g, G, lin, c->w_q.template as<Real>(), lout);
+        break;
+    case OP_RADON: launch_radon<Real, V>(g, G, lin, lout, c->stream); break;
+    case OP_RADON_ADJ: launch_radon_adjoint<Real, V>(g, G, lin, lout, c->stream); break;
+    case OP_FILTER: lanes_filter<Real, V>(c, g, G, lin, lout); break;
+    case OP_BACKPROJECT: launch_backproject<Real, V>(g, G, lin, lout, c->stream); break;
+    }
+    CKLAUNCH(c);
+    if constexpr (V > 1) {
+        launch_from_lanes<Real, V>(lout, out, S, nout, c->stream);
+        CKLAUNCH(c);
+    }
+    return ACU_OK;
+}
+
+template <typename Real>
+int run_op(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
+{
+    CKRET(check_ctx(c, S));
+    if (S == 0) return ACU_OK;
+    if (!in || !out) return set_err(c, ACU_ERR_INVALID, "null array");
+    if constexpr (sizeof(Real) == 4) {
+        if (pick_lanes(c, S, false) == 4) return run_op_v<Real, 4>(c, op, S, in, out);
+    }
+    return run_op_v<Real, 1>(c, op, S, in, out);
+}
+
+// Host-buffer wrapper: copy in, run on the device, copy out, synchronise.
+int run_op_host(acu_ctx* c, OpKind op, int S, const float* in, float* out)
+{
+    CKRET(check_ctx(c, S));
+    if (S == 0) return ACU_OK;
+    if (!in || !out) return set_err(c, ACU_ERR_INVALID, "null array");
+    const size_t nsino = (size_t)c->T * c->N, nimg = (size_t)c->N * c->N;
+    const size_t nin = (op == OP_RADON ? nimg : nsino) * S;
+    const size_t nout = (op == OP_RADON || op == OP_FILTER ? nsino : nimg) * S;
+    CK(c, c->w_host_in.ensure(sizeof(float) * nin));
+    CK(c, c->w_host_out.ensure(sizeof(float) * nout));
+    CK(c, cudaMemcpyAsync(c->w_host_in.p, in, sizeof(float) * nin, cudaMemcpyHostToDevice, c->stream));
+    CKRET(run_op<float>(c, op, S, c->w_host_in.template as<float>(), c->w_host_out.template as<float>()));
+    CK(c, cudaMemcpyAsync(out, c->w_host_out.p, sizeof(float) * nout, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return ACU_OK;
+}
+
+// ---- batched split-Bregman TV (tomography/tv_hpc.F90:162-363) --------------
+template <typename Real>
+TvState<Real>& tvstate(acu_ctx* c);
+template <>
+TvState<float>& tvstate<float>(acu_ctx* c) { return c->tv32; }
+template <>
+TvState<double>& tvstate<double>(acu_ctx* c) { return c->tv64; }
+
+template <typename Real, int V>
+struct TvRun {
+    acu_ctx* c;
+    const DevGeom<Real>* g;
+    TvState<Real>* s;
+    int N, T, G, S, ninner, ncg;
+    Real lambda, mu;
+    bool verbose;
+    TvScalars sc;
+    size_t nimg() const { return (size_t)N * N * G * V; }
+    size_t nsino() const { return (size_t)T * N * G * V; }
+    Real* B(DevBuf& b) const { return b.template as<Real>(); }
+
+    void iradon(const Real* sino, Real* img) { lanes_iradon<Real, V>(c, *g, G, sino, B(s->q), img); }
+    void radon(const Real* img, Real* sino) { launch_radon<Real, V>(*g, G, img, sino, c->stream); }
+
+    // One Bregman outer iteration (tv_hpc.F90:206-346).  On entry ruk holds
+    // radon(uk) for the current uk, which the first inner iteration reuses.
+    void outer_body()
+    {
+        cudaStream_t st = c->stream;
+        using E = TvEw<Real, V>;
+        for (int jinner = 1; jinner <= ninner; ++jinner) {
+            if (verbose) cudaMemcpyAsync(s->ukp.p, s->uk.p, sizeof(Real) * nimg(), cudaMemcpyDeviceToDevice, st);
+            iradon(B(s->fk), B(s->tmp));                                   // ifkt
+            E::rhs(N, G, mu, lambda, B(s->tmp), B(s->dx), B(s->bx), B(s->dy), B(s->by), B(s->rhs), st);
+            if (jinner > 1) radon(B(s->uk), B(s->ruk));
+            iradon(B(s->ruk), B(s->tmp));                                  // iukt
+            E::resid(N, G, mu, lambda, B(s->rhs), B(s->tmp), B(s->uk), B(s->r), B(s->p), sc, st);
+            launch_cg_finalize(0, G * V, sc, st);
+            for (int k = 0; k < ncg; ++k) {
+                radon(B(s->p), B(s->rp));
+                iradon(B(s->rp), B(s->tmp));                               // irpt
+                E::apply(N, G, mu, lambda, B(s->tmp), B(s->p), B(s->Ap), sc, st);
+                launch_cg_finalize(1, G * V, sc, st);
+                E::update(N, G, B(s->p), B(s->Ap), B(s->uk), B(s->r), sc, st);
+                launch_cg_finalize(2, G * V, sc, st);
+                E::pupdate(N, G, B(s->r), B(s->p), sc, st);
+            }
+            E::shrink(N, G, lambda, B(s->uk), B(s->dx), B(s->bx), B(s->dy), B(s->by),
+                      verbose ? B(s->ukp) : nullptr, sc, st);
+            if (verbose) launch_cg_finalize(3, G * V, sc, st);
+        }
+        radon(B(s->uk), B(s->ruk));
+        E::fk_update(nsino(), B(s->fk), B(s->f), B(s->ruk), st);
+    }
+};
+
+template <typename Real, int V>
+int tv_solve_v(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int ncg, Real lambda, Real mu,
+               Real* d_tv, Real* d_fbp)
+{
+    CKRET(ensure_geom<Real>(c));
+    TvState<Real>& s = tvstate<Real>(c);
+    const int N = c->N, T = c->T, G = (S + V - 1) / V;
+    const size_t nimg = (size_t)N * N * G * V, nsino = (size_t)T * N * G * V;
+    for (DevBuf* b : {&s.f, &s.fk, &s.ruk, &s.rp, &s.q}) CK(c, b->ensure(sizeof(Real) * nsino));
+    for (DevBuf* b : {&s.uk, &s.dx, &s.dy, &s.bx, &s.by, &s.rhs, &s.r, &s.p, &s.Ap, &s.tmp})
+        CK(c, b->ensure(sizeof(Real) * nimg));
+    if (c->opt_verbose) CK(c, s.ukp.ensure(sizeof(Real) * nimg));
+    const int Sp = G * V;
+    const int nblk = (int)std::min<size_t>(((size_t)N * N + 255) / 256, 512);
+    for (DevBuf* b : {&s.rsold, &s.alpha, &s.beta, &s.delta}) CK(c, b->ensure(sizeof(double) * Sp));
+    CK(c, s.part.ensure(sizeof(double) * (size_t)nblk * Sp));
+
+    TvRun<Real, V> run;
+    run.c = c;
+    run.g = &geomset<Real>(c).d;
+    run.s = &s;
+    run.N = N; run.T = T; run.G = G; run.S = S;
+    run.ninner = ninner; run.ncg = ncg; run.lambda = lambda; run.mu = mu;
+    run.verbose = c->opt_verbose != 0;
+    run.sc = TvScalars{s.rsold.template as<double>(), s.alpha.template as<double>(), s.beta.template as<double>(), s.delta.template as<double>(),
+                       s.part.template as<double>(), nblk};
+    cudaStream_t st = c->stream;
+
+    // warm start and state initialisation (tv_hpc.F90:172-202)
+    if constexpr (V > 1)
+        launch_to_lanes<Real, V>(d_f, s.f.template as<Real>(), S, (size_t)T * N, st);
+    else
+        CK(c, cudaMemcpyAsync(s.f.p, d_f, sizeof(Real) * nsino, cudaMemcpyDeviceToDevice, st));
+    run.iradon(s.f.template as<Real>(), s.uk.template as<Real>());
+    if (d_fbp) {
+        if constexpr (V > 1)
+            launch_from_lanes<Real, V>(s.uk.template as<Real>(), d_fbp, S, (size_t)N * N, st);
+        else
+            CK(c, cudaMemcpyAsync(d_fbp, s.uk.p, sizeof(Real) * nimg, cudaMemcpyDeviceToDevice, st));
+    }
+    for (DevBuf* b : {&s.dx, &s.dy, &s.bx, &s.by}) CK(c, cudaMemsetAsync(b->p, 0, sizeof(Real) * nimg, st));
+    CK(c, cudaMemcpyAsync(s.fk.p, s.f.p, sizeof(Real) * nsino, cudaMemcpyDeviceToDevice, st));
+    run.radon(s.uk.template as<Real>(), s.ruk.template as<Real>());
+    CKLAUNCH(c);
+
+    const bool use_graph = c->opt_graph != 0 && !run.verbose && nouter > 1;
+    if (use_graph) {
+        char key[256];
+        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.9g/%.9g/%d/%p/%p", (int)sizeof(Real), V, G, ninner, ncg,
+                 (double)lambda, (double)mu, c->opt_filter, s.uk.p, (void*)st);
+        if (!s.graph || s.graph_key != key) {
+            if (s.graph) {
+                cudaGraphExecDestroy(s.graph);
+                s.graph = nullptr;
+            }
+            // Capture on the context's private stream (the legacy stream
+            // cannot be captured); the graph is then launched on `st`.
+            cudaGraph_t graph;
+            CK(c, cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal));
+            c->stream = c->own_stream;
+            run.outer_body();
+            c->stream = st;
+            cudaError_t e = cudaStreamEndCapture(c->own_stream, &graph);
+            if (e != cudaSuccess) return set_err(c, ACU_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&s.graph, graph, 0);
+            cudaGraphDestroy(graph);
+            if (e != cudaSuccess) {
+                s.graph = nullptr;
+                return set_err(c, ACU_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+            }
+            s.graph_key = key;
+        }
+        for (int jo = 0; jo < nouter; ++jo) CK(c, cudaGraphLaunch(s.graph, st));
+    } else {
+        c->last_delta.assign(S, 0.0);
+        for (int jo = 1; jo <= nouter; ++jo) {
+            run.outer_body();
+            CKLAUNCH(c);
+            if (run.verbose && (jo % c->opt_print_every == 0 || jo == nouter)) {
+                std::vector<double> dl(Sp);
+                CK(c, cudaMemcpyAsync(dl.data(), s.delta.p, sizeof(double) * Sp, cudaMemcpyDeviceToHost, st));
+                CK(c, cudaStreamSynchronize(st));
+                for (int k = 0; k < S; ++k) c->last_delta[k] = dl[k];
+                if (jo % c->opt_print_every == 0)
+                    for (int k = 0; k < S; ++k)
+                        printf(" Slice: %12d Loop: %12d delta: %15.8E\n", c->opt_slice_base + k, jo, dl[k]);
+                fflush(stdout);
+            }
+        }
+    }
+    if constexpr (V > 1)
+        launch_from_lanes<Real, V>(s.uk.template as<Real>(), d_tv, S, (size_t)N * N, st);
+    else
+        CK(c, cudaMemcpyAsync(d_tv, s.uk.p, sizeof(Real) * nimg, cudaMemcpyDeviceToDevice, st));
+    CKLAUNCH(c);
+    return ACU_OK;
+}
+
+template <typename Real>
+int tv_solve(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int ncg, Real lambda, Real mu,
+             Real* d_tv, Real* d_fbp)
+{
+    CKRET(check_ctx(c, S));
+    if (S == 0) return ACU_OK;
+    if (!d_f || !d_tv) return set_err(c, ACU_ERR_INVALID, "null array");
+    if (ninner < 0 || nouter < 0 || ncg < 0)
+        return set_err(c, ACU_ERR_INVALID, "iteration counts must be >= 0");
+    if (lambda == Real(0)) return set_err(c, ACU_ERR_INVALID, "lambda must be non-zero (shrink threshold 1/lambda)");
+    if constexpr (sizeof(Real) == 4) {
+        if (pick_lanes(c, S, false) == 4)
+            return tv_solve_v<Real, 4>(c, S, d_f, ninner, nouter, ncg, lambda, mu, d_tv, d_fbp);
+    }
+    return tv_solve_v<Real, 1>(c, S, d_f, ninner, nouter, ncg, lambda, mu, d_tv, d_fbp);
+}
+
+// ---- per-slice comparator: the reference's loop structure on the GPU ---------
+// One slice at a time, one kernel per OpenACC region of tv_hpc.F90:162-363,
+// direct filter, radon(uk) recomputed where the reference recomputes it, and
+// the CG reductions read back to the host every step (the reference computes
+// alpha and beta on the host).
+int tv_plain(acu_ctx* c, int S, const float* d_f, int ninner, int nouter, int ncg, float lambda, float mu,
+             float* d_tv, float* d_fbp)
+{
+    CKRET(check_ctx(c, S));
+    if (S == 0) return ACU_OK;
+    if (!d_f || !d_tv) return set_err(c, ACU_ERR_INVALID, "null array");
+    if (lambda == 0.0f) return set_err(c, ACU_ERR_INVALID, "lambda must be non-zero (shrink threshold 1/lambda)");
+    CKRET(ensure_geom<float>(c));
+    const DevGeom<float>& g = c->g32.d;
+    TvState<float>& s = c->tv32;
+    const int N = c->N, T = c->T;
+    const size_t nimg = (size_t)N * N, nsino = (size_t)T * N;
+    for (DevBuf* b : {&s.fk, &s.ruk, &s.rp, &s.q}) CK(c, b->ensure(sizeof(float) * nsino));
+    for (DevBuf* b : {&s.uk, &s.ukp, &s.dx, &s.dy, &s.bx, &s.by, &s.rhs, &s.r, &s.p, &s.Ap, &s.tmp})
+        CK(c, b->ensure(sizeof(float) * nimg));
+    const int nblk = (int)std::min<size_t>((nimg + 255) / 256, 512);
+    for (DevBuf* b : {&s.rsold, &s.alpha, &s.beta, &s.delta}) CK(c, b->ensure(sizeof(double) * 1));
+    CK(c, s.part.ensure(sizeof(double) * (size_t)nblk));
+    TvScalars sc{s.rsold.template as<double>(), s.alpha.template as<double>(), s.beta.template as<double>(), s.delta.template as<double>(),
+                 s.part.template as<double>(), nblk};
+    cudaStream_t st = c->stream;
+    using E = TvEw<float, 1>;
+    auto F = [](DevBuf& b) { return b.template as<float>(); };
+    auto iradon = [&](const float* in, float* out) {
+        launch_filter_direct<float, 1>(g, 1, in, F(s.q), st);
+        launch_backproject<float, 1>(g, 1, F(s.q), out, st);
+    };
+    auto radon = [&](const float* in, float* out) { launch_radon<float, 1>(g, 1, in, out, st); };
+    double host_scalar;
+    c->last_delta.assign(S, 0.0);
+    for (int sl = 0; sl < S; ++sl) {
+        const float* f = d_f + (size_t)sl * nsino;
+        iradon(f, F(s.uk));
+        if (d_fbp) CK(c, cudaMemcpyAsync(d_fbp + (size_t)sl * nimg, s.uk.p, sizeof(float) * nimg,
+                                         cudaMemcpyDeviceToDevice, st));
+        for (DevBuf* b : {&s.dx, &s.dy, &s.bx, &s.by}) CK(c, cudaMemsetAsync(b->p, 0, sizeof(float) * nimg, st));
+        CK(c, cudaMemcpyAsync(s.fk.p, f, sizeof(float) * nsino, cudaMemcpyDeviceToDevice, st));
+        for (int jo = 1; jo <= nouter; ++jo) {
+            for (int ji = 1; ji <= ninner; ++ji) {
+                CK(c, cudaMemcpyAsync(s.ukp.p, s.uk.p, sizeof(float) * nimg, cudaMemcpyDeviceToDevice, st));
+                iradon(F(s.fk), F(s.tmp));
+                E::rhs(N, 1, mu, lambda, F(s.tmp), F(s.dx), F(s.bx), F(s.dy), F(s.by), F(s.rhs), st);
+                radon(F(s.uk), F(s.ruk));
+                iradon(F(s.ruk), F(s.tmp));
+                E::resid(N, 1, mu, lambda, F(s.rhs), F(s.tmp), F(s.uk), F(s.r), F(s.p), sc, st);
+                launch_cg_finalize(0, 1, sc, st);
+                CK(c, cudaMemcpyAsync(&host_scalar, s.rsold.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+                CK(c, cudaStreamSynchronize(st));
+                for (int k = 0; k < ncg; ++k) {
+                    radon(F(s.p), F(s.rp));
+                    iradon(F(s.rp), F(s.tmp));
+                    E::apply(N, 1, mu, lambda, F(s.tmp), F(s.p), F(s.Ap), sc, st);
+                    launch_cg_finalize(1, 1, sc, st);
+                    CK(c, cudaMemcpyAsync(&host_scalar, s.alpha.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+                    CK(c, cudaStreamSynchronize(st));
+                    E::update(N, 1, F(s.p), F(s.Ap), F(s.uk), F(s.r), sc, st);
+                    launch_cg_finalize(2, 1, sc, st);
+                    CK(c, cudaMemcpyAsync(&host_scalar, s.beta.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+                    CK(c, cudaStreamSynchronize(st));
+                    E::pupdate(N, 1, F(s.r), F(s.p), sc, st);
+                }
+                E::shrink(N, 1, lambda, F(s.uk), F(s.dx), F(s.bx), F(s.dy), F(s.by), F(s.ukp), sc, st);
+                launch_cg_finalize(3, 1, sc, st);
+            }
+            radon(F(s.uk), F(s.ruk));
+            E::fk_update(nsino, F(s.fk), f, F(s.ruk), st);
+            CKLAUNCH(c);
+            if (c->opt_verbose && jo % c->opt_print_every == 0) {
+                CK(c, cudaMemcpyAsync(&host_scalar, s.delta.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+                CK(c, cudaStreamSynchronize(st));
+                printf(" Slice: %12d Loop: %12d delta: %15.8E\n", c->opt_slice_base + sl, jo, host_scalar);
+                fflush(stdout);
+            }
+        }
+        CK(c, cudaMemcpyAsync(d_tv + (size_t)sl * nimg, s.uk.p, sizeof(float) * nimg, cudaMemcpyDeviceToDevice, st));
+        CK(c, cudaMemcpyAsync(&host_scalar, s.delta.p, sizeof(double), cudaMemcpyDeviceToHost, st));
+        CK(c, cudaStreamSynchronize(st));
+        c->last_delta[sl] = host_scalar;
+    }
+    return ACU_OK;
+}
+
+int tv_host(acu_ctx* c, bool plain, int S, const float* f, int ninner, int nouter, int ncg, float lambda,
+            float mu, float* tv, float* fbp)
+{
+    CKRET(check_ctx(c, S));
+    if (S == 0) return ACU_OK;
+    if (!f || !tv) return set_err(c, ACU_ERR_INVALID, "null array");
+    const size_t nsino = (size_t)c->T * c->N * S, nimg = (size_t)c->N * c->N * S;
+    CK(c, c->w_host_in.ensure(sizeof(float) * nsino));
+    CK(c, c->w_host_out.ensure(sizeof(float) * nimg * (fbp ? 2 : 1)));
+    float* d_tv = c->w_host_out.template as<float>();
+    float* d_fbp = fbp ? d_tv + nimg : nullptr;
+    CK(c, cudaMemcpyAsync(c->w_host_in.p, f, sizeof(float) * nsino, cudaMemcpyHostToDevice, c->stream));
+    if (plain)
+        CKRET(tv_plain(c, S, c->w_host_in.template as<float>(), ninner, nouter, ncg, lambda, mu, d_tv, d_fbp));
+    else
+        CKRET(tv_solve<float>(c, S, c->w_host_in.template as<float>(), ninner, nouter, ncg, lambda, mu, d_tv, d_fbp));
+    CK(c, cudaMemcpyAsync(tv, d_tv, sizeof(float) * nimg, cudaMemcpyDeviceToHost, c->stream));
+    if (fbp) CK(c, cudaMemcpyAsync(fbp, d_fbp, sizeof(float) * nimg, cudaMemcpyDeviceToHost, c->stream));
+    CK(c, cudaStreamSynchronize(c->stream));
+    return ACU_OK;
+}
+
+}  // namespace
+
+// =============================================================================
+// exported C ABI
+// =============================================================================
+extern "C" {
+
+int acu_ctx_create(acu_ctx** out, int nimage, int ntheta, const float* theta_deg, int wpu)
+{
+    if (!out) return set_err(nullptr, ACU_ERR_INVALID, "null output pointer");
+    *out = nullptr;
+    if (nimage < 0 || (nimage > 0 && (nimage < 3 || ntheta < 1 || !theta_deg)))
+        return set_err(nullptr, ACU_ERR_INVALID, "invalid geometry: nimage=%d ntheta=%d theta=%p", nimage,
+                       ntheta, (const void*)theta_deg);
+    if (nimage > 46340)
+        return set_err(nullptr, ACU_ERR_INVALID, "nimage=%d exceeds the supported maximum 46340", nimage);
+    std::unique_ptr<acu_ctx> c(new (std::nothrow) acu_ctx());
+    if (!c) return set_err(nullptr, ACU_ERR_NOMEM, "host allocation failed");
+    c->N = nimage;
+    c->T = nimage > 0 ? ntheta : 0;
+    c->wpu = wpu;
+    if (nimage > 0) c->theta.assign(theta_deg, theta_deg + ntheta);
+    cudaError_t e = cudaStreamCreateWithFlags(&c->own_stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess)
+        return set_err(nullptr, ACU_ERR_CUDA, "cudaStreamCreate failed: %s", cudaGetErrorString(e));
+    c->stream = nullptr;  // the legacy default stream until acu_set_stream
+    *out = c.release();
+    return ACU_OK;
+}
+
+int acu_ctx_destroy(acu_ctx* c)
+{
+    if (!c) return ACU_OK;
+    cudaStreamSynchronize(c->stream);
+    cudaStream_t own = c->own_stream;
+    delete c;
+    if (own) cudaStreamDestroy(own);
+    return ACU_OK;
+}
+
+const char* acu_last_error(const acu_ctx* c)
+{
+    if (c) return c->err.c_str();
+    return g_last_error.c_str();
+}
+
+int acu_set_stream(acu_ctx* c, void* stream)
+{
+    if (!c) return set_err(nullptr, ACU_ERR_INVALID, "null context");
+    c->stream = (cudaStream_t)stream;  // NULL: the legacy default stream
+    return ACU_OK;
+}
+
+int acu_set_option(acu_ctx* c, int option, int value)
+{
+    if (!c) return set_err(nullptr, ACU_ERR_INVALID, "null context");
+    switch (option) {
+    case ACU_OPT_FILTER:
+        if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_FILTER must be 0 or 1");
+        c->opt_filter = value;
+        return ACU_OK;
+    case ACU_OPT_LANES:
+        if (value != 0 && value != 1 && value != 4)
+            return set_err(c, ACU_ERR_INVALID, "ACU_OPT_LANES must be 0, 1 or 4");
+        c->opt_lanes = value;
+        return ACU_OK;
+    case ACU_OPT_GRAPH: c->opt_graph = value != 0; return ACU_OK;
+    case ACU_OPT_VERBOSE: c->opt_verbose = value != 0; return ACU_OK;
+    case ACU_OPT_PRINT_EVERY:
+        if (value < 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PRINT_EVERY must be >= 1");
+        c->opt_print_every = value;
+        return ACU_OK;
+    case 6: c->opt_slice_base = value; return ACU_OK;
+    }
+    return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
+}
+
+int acu_get_option(const acu_ctx* c, int option, int* value)
+{
+    if (!c || !value) return set_err(nullptr, ACU_ERR_INVALID, "null argument");
+    switch (option) {
+    case ACU_OPT_FILTER: *value = c->opt_filter; return ACU_OK;
+    case ACU_OPT_LANES: *value = c->opt_lanes; return ACU_OK;
+    case ACU_OPT_GRAPH: *value = c->opt_graph; return ACU_OK;
+    case ACU_OPT_VERBOSE: *value = c->opt_verbose; return ACU_OK;
+    case ACU_OPT_PRINT_EVERY: *value = c->opt_print_every; return ACU_OK;
+    case 6: *value = c->opt_slice_base; return ACU_OK;
+    }
+    return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);
+}
+
+int acu_iradon(acu_ctx* c, int S, const float* sino, float* img) { return run_op_host(c, OP_IRADON, S, sino, img); }
+int acu_radon(acu_ctx* c, int S, const float* img, float* sino) { return run_op_host(c, OP_RADON, S, img, sino); }
+int acu_radon_adjoint(acu_ctx* c, int S, const float* sino, float* img)
+{
+    return run_op_host(c, OP_RADON_ADJ, S, sino, img);
+}
+int acu_iradon_dev(acu_ctx* c, int S, const float* s, float* i) { return run_op<float>(c, OP_IRADON, S, s, i); }
+int acu_radon_dev(acu_ctx* c, int S, const float* i, float* s) { return run_op<float>(c, OP_RADON, S, i, s); }
+int acu_radon_adjoint_dev(acu_ctx* c, int S, const float* s, float* i)
+{
+    return run_op<float>(c, OP_RADON_ADJ, S, s, i);
+}
+int acu_filter_dev(acu_ctx* c, int S, const float* s, float* o) { return run_op<float>(c, OP_FILTER, S, s, o); }
+int acu_backproject_dev(acu_ctx* c, int S, const float* q, float* i)
+{
+    return run_op<float>(c, OP_BACKPROJECT, S, q, i);
+}
+int acu_iradon_dev_f64(acu_ctx* c, int S, const double* s, double* i) { return run_op<double>(c, OP_IRADON, S, s, i); }
+int acu_radon_dev_f64(acu_ctx* c, int S, const double* i, double* s) { return run_op<double>(c, OP_RADON, S, i, s); }
+int acu_radon_adjoint_dev_f64(acu_ctx* c, int S, const double* s, double* i)
+{
+    return run_op<double>(c, OP_RADON_ADJ, S, s, i);
+}
+
+int acu_tvopt(acu_ctx* c, int S, const float* f, int ninner, int nouter, int ncg, float lambda, float mu,
+              float* tv, float* fbp)
+{
+    return tv_host(c, false, S, f, ninner, nouter, ncg, lambda, mu, tv, fbp);
+}
+int acu_tvopt_dev(acu_ctx* c, int S, const float* f, int ninner, int nouter, int ncg, float lambda, float mu,
+                  float* tv, float* fbp)
+{
+    return tv_solve<float>(c, S, f, ninner, nouter, ncg, lambda, mu, tv, fbp);
+}
+int acu_tvopt_plain(acu_ctx* c, int S, const float* f, int ninner, int nouter, int ncg, float lambda, float mu,
+                    float* tv, float* fbp)
+{
+    return tv_host(c, true, S, f, ninner, nouter, ncg, lambda, mu, tv, fbp);
+}
+int acu_tvopt_plain_dev(acu_ctx* c, int S, const float* f, int ninner, int nouter, int ncg, float lambda,
+                        float mu, float* tv, float* fbp)
+{
+    return tv_plain(c, S, f, ninner, nouter, ncg, lambda, mu, tv, fbp);
+}
+int acu_tvopt_dev_f64(acu_ctx* c, int S, const double* f, int ninner, int nouter, int ncg, double lambda,
+                      double mu, double* tv, double* fbp)
+{
+    return tv_solve<double>(c, S, f, ninner, nouter, ncg, lambda, mu, tv, fbp);
+}
+
+int acu_tv_last_delta(const acu_ctx* c, int S, double* delta)
+{
+    if (!c || !delta) return set_err(nullptr, ACU_ERR_INVALID, "null argument");
+    for (int k = 0; k < S; ++k) delta[k] = k < (int)c->last_delta.size() ? c->last_delta[k] : 0.0;
+    return ACU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,81 @@
+// Internal launcher declarations shared by the .cu translation units.
+#pragma once
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+namespace acu {
+
+// Geometry of one reconstruction grid on the device, for one precision.
+// All tables are computed on the host (tables.cpp) with the reference's
+// arithmetic and uploaded once.
+template <typename Real>
+struct DevGeom {
+    int N = 0, T = 0;
+    Real mid = 0;                 // (N+1)/2, integer division (tv_hpc.F90:15)
+    const Real* sc_bp = nullptr;  // [T][2] sin, cos of pi*(90-theta)/180
+    const Real* sc_fp = nullptr;  // [T][2] sin, cos of pi*(theta-90)/180
+    const Real* filt = nullptr;   // [2N+1] filter taps (tv_hpc.F90:53-56)
+    const Real* cmask = nullptr;  // [N][N] tapered mask times pi/T (tv_hpc.F90:58-74)
+    const Real* fft_h = nullptr;  // [L] real spectrum of the wrapped filter
+    const float2* fft_tw = nullptr; // [L/2] twiddles exp(-2 pi i k / L) (float)
+    const double2* fft_tw64 = nullptr;
+    int fft_L = 0, fft_log2L = 0;
+};
+
+// ---- radon operators (kernels_radon.cu); arrays in lane layout ------------
+template <typename Real, int V>
+void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st);
+template <typename Real, int V>
+void launch_radon(const DevGeom<Real>& g, int G, const Real* img, Real* sino, cudaStream_t st);
+template <typename Real, int V>
+void launch_radon_adjoint(const DevGeom<Real>& g, int G, const Real* sino, Real* img, cudaStream_t st);
+template <typename Real, int V>
+void launch_filter_direct(const DevGeom<Real>& g, int G, const Real* sino, Real* out, cudaStream_t st);
+template <typename Real, int V>
+void launch_filter_fft(const DevGeom<Real>& g, int G, const Real* sino, Real* out, cudaStream_t st);
+template <typename Real>
+bool fft_fits(int L);
+
+// ---- layout conversion (kernels_tv.cu) ------------------------------------
+// plain [S][npos] <-> lanes [G][npos][V]; slices >= S of the last group are 0.
+template <typename Real, int V>
+void launch_to_lanes(const Real* plain, Real* lanes, int S, size_t npos, cudaStream_t st);
+template <typename Real, int V>
+void launch_from_lanes(const Real* lanes, Real* plain, int S, size_t npos, cudaStream_t st);
+template <typename Real>
+void launch_convert(const float* in, Real* out, size_t n, cudaStream_t st);
+
+// ---- split-Bregman / CG elementwise steps (kernels_tv.cu) ----------------
+// All images are [G][N][N][V]; per-slice scalars are double[G*V].
+struct TvScalars {
+    double* rsold;   // [S]
+    double* alpha;   // [S]
+    double* beta;    // [S]
+    double* delta;   // [S] Err_diff
+    double* part;    // [nblk_max * S] block partial sums
+    int nblk;        // blocks of the elementwise grid
+};
+
+template <typename Real, int V>
+struct TvEw {
+    static void rhs(int N, int G, Real mu, Real lambda, const Real* ifkt, const Real* dx,
+                    const Real* bx, const Real* dy, const Real* by, Real* rhs, cudaStream_t st);
+    static void resid(int N, int G, Real mu, Real lambda, const Real* rhs, const Real* iukt,
+                      const Real* uk, Real* r, Real* p, const TvScalars& sc, cudaStream_t st);
+    static void apply(int N, int G, Real mu, Real lambda, const Real* irpt, const Real* p,
+                      Real* Ap, const TvScalars& sc, cudaStream_t st);
+    static void update(int N, int G, const Real* p, const Real* Ap, Real* uk, Real* r,
+                       const TvScalars& sc, cudaStream_t st);
+    static void pupdate(int N, int G, const Real* r, Real* p, const TvScalars& sc, cudaStream_t st);
+    static void shrink(int N, int G, Real lambda, const Real* uk, Real* dx, Real* bx, Real* dy,
+                       Real* by, const Real* ukp, const TvScalars& sc, cudaStream_t st);
+    static void fk_update(size_t n, Real* fk, const Real* f, const Real* ruk, cudaStream_t st);
+};
+
+// Finalisers of the FP64 CG scalars (one block per slice, fixed order).
+// which: 0 -> rsold = sum;  1 -> alpha = rsold / sum;  2 -> beta = sum / rsold,
+// rsold = sum;  3 -> delta = sum.
+void launch_cg_finalize(int which, int S, const TvScalars& sc, cudaStream_t st);
+
+}  // namespace acu

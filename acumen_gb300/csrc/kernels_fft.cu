@@ -1,0 +1,176 @@
+// FFT form of iradon's ramp filter (tomography/tv_hpc.F90:93-105).
+//
+// The reference convolves every sinogram column directly with the 2N+1 taps
+// (O(N^2) per column).  Here each block packs two real columns into one
+// complex signal z = a + i b, zero-pads it to L >= 2N-2 (a power of two),
+// and computes y = IFFT(H . FFT(z)) with H the real spectrum of the wrapped,
+// symmetric tap sequence (computed in double on the host, 1/L folded in).
+// Because H is real, Re(y) and Im(y) are the two filtered columns.  The
+// transforms are radix-4 Stockham stages (a radix-2 stage last when log2 L is
+// odd) in shared memory with a double-precision-built twiddle table.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace acu {
+
+template <typename Real>
+struct Cplx;
+template <>
+struct Cplx<float> {
+    using T = float2;
+};
+template <>
+struct Cplx<double> {
+    using T = double2;
+};
+
+template <typename C>
+__device__ __forceinline__ C cmul(C a, C b)
+{
+    C r;
+    r.x = a.x * b.x - a.y * b.y;
+    r.y = a.x * b.y + a.y * b.x;
+    return r;
+}
+template <typename C>
+__device__ __forceinline__ C cadd(C a, C b)
+{
+    C r;
+    r.x = a.x + b.x;
+    r.y = a.y + b.y;
+    return r;
+}
+template <typename C>
+__device__ __forceinline__ C csub(C a, C b)
+{
+    C r;
+    r.x = a.x - b.x;
+    r.y = a.y - b.y;
+    return r;
+}
+
+// Forward DFT of length L (power of two >= 16) held in d0; returns the buffer
+// holding the natural-order result (d0 or d1).
+template <typename C>
+__device__ C* fft_stockham(C* d0, C* d1, const C* __restrict__ tw, int L)
+{
+    for (int Ns = 1; Ns < L;) {
+        const int R = ((L / Ns) % 4 == 0) ? 4 : 2;
+        const int stride = L / (Ns * R);
+        const int nb = L / R;
+        for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+            const int k = j % Ns;
+            const int idxD = (j / Ns) * Ns * R + k;
+            if (R == 4) {
+                C v0 = d0[j];
+                C v1 = cmul(d0[j + nb], tw[k * stride]);
+                C v2 = cmul(d0[j + 2 * nb], tw[2 * k * stride]);
+                C v3 = cmul(d0[j + 3 * nb], tw[3 * k * stride]);
+                C a = cadd(v0, v2), b = csub(v0, v2), c = cadd(v1, v3), e = csub(v1, v3);
+                C d;               // e * (-i)
+                d.x = e.y;
+                d.y = -e.x;
+                d1[idxD] = cadd(a, c);
+                d1[idxD + Ns] = cadd(b, d);
+                d1[idxD + 2 * Ns] = csub(a, c);
+                d1[idxD + 3 * Ns] = csub(b, d);
+            } else {
+                C v0 = d0[j];
+                C v1 = cmul(d0[j + nb], tw[k * stride]);
+                d1[idxD] = cadd(v0, v1);
+                d1[idxD + Ns] = csub(v0, v1);
+            }
+        }
+        __syncthreads();
+        C* t = d0;
+        d0 = d1;
+        d1 = t;
+        Ns *= R;
+    }
+    return d0;
+}
+
+// One block filters two real columns: (a, b) with element n at a[n*stride],
+// b[n*stride] (b may be null: treated as zero and not written).
+template <typename Real>
+__global__ void __launch_bounds__(256) k_filter_fft(const Real* __restrict__ sino, Real* __restrict__ out,
+                                                    const Real* __restrict__ H,
+                                                    const typename Cplx<Real>::T* __restrict__ tw, int N, int T,
+                                                    int L, int V)
+{
+    using C = typename Cplx<Real>::T;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    C* d0 = reinterpret_cast<C*>(smem_raw);
+    C* d1 = d0 + L;
+    const int g = blockIdx.y;
+    size_t offa, offb;
+    int stride;
+    bool has_b = true;
+    if (V == 4) {
+        const int t = blockIdx.x >> 1, h = blockIdx.x & 1;
+        offa = (((size_t)g * T + t) * N) * 4 + 2 * h;
+        offb = offa + 1;
+        stride = 4;
+    } else {
+        const int t0 = 2 * blockIdx.x;
+        offa = ((size_t)g * T + t0) * N;
+        offb = offa + N;
+        stride = 1;
+        has_b = (t0 + 1) < T;
+    }
+    for (int n = threadIdx.x; n < L; n += blockDim.x) {
+        C z;
+        z.x = n < N ? sino[offa + (size_t)n * stride] : Real(0);
+        z.y = (n < N && has_b) ? sino[offb + (size_t)n * stride] : Real(0);
+        d0[n] = z;
+    }
+    __syncthreads();
+    C* res = fft_stockham<C>(d0, d1, tw, L);
+    C* other = (res == d0) ? d1 : d0;
+    // W = H/L * conj(Z); y = conj(FFT(W))
+    for (int m = threadIdx.x; m < L; m += blockDim.x) {
+        C z = res[m];
+        const Real h = H[m];
+        C w;
+        w.x = h * z.x;
+        w.y = -h * z.y;
+        res[m] = w;
+    }
+    __syncthreads();
+    C* y = fft_stockham<C>(res, other, tw, L);
+    for (int n = threadIdx.x; n < N; n += blockDim.x) {
+        const C v = y[n];
+        out[offa + (size_t)n * stride] = v.x;
+        if (has_b) out[offb + (size_t)n * stride] = -v.y;
+    }
+}
+
+template <typename Real, int V>
+void launch_filter_fft(const DevGeom<Real>& g, int G, const Real* sino, Real* out, cudaStream_t st)
+{
+    using C = typename Cplx<Real>::T;
+    const size_t sm = 2 * (size_t)g.fft_L * sizeof(C);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_filter_fft<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+        attr_set = true;
+    }
+    const C* tw = reinterpret_cast<const C*>(sizeof(Real) == 4 ? (const void*)g.fft_tw : (const void*)g.fft_tw64);
+    dim3 grd(V == 4 ? 2 * g.T : (g.T + 1) / 2, G);
+    k_filter_fft<Real><<<grd, 256, sm, st>>>(sino, out, g.fft_h, tw, g.N, g.T, g.fft_L, V);
+}
+
+// Largest FFT length whose two shared-memory buffers fit in one block.
+template <typename Real>
+bool fft_fits(int L)
+{
+    return 2 * (size_t)L * 2 * sizeof(Real) <= 227 * 1024;
+}
+
+template void launch_filter_fft<float, 1>(const DevGeom<float>&, int, const float*, float*, cudaStream_t);
+template void launch_filter_fft<float, 4>(const DevGeom<float>&, int, const float*, float*, cudaStream_t);
+template void launch_filter_fft<double, 1>(const DevGeom<double>&, int, const double*, double*, cudaStream_t);
+template bool fft_fits<float>(int);
+template bool fft_fits<double>(int);
+
+}  // namespace acu

@@ -1,0 +1,266 @@
+// Radon-transform kernels: pixel-driven backprojection (iradon's second half),
+// the bilinear ray-sum projector (radon), its exact transpose, and the direct
+// ramp-filter convolution (iradon's first half).
+//
+// Arrays are in lane layout (common.cuh): V slices of one group interleaved,
+// so each thread carries V slices through one geometry evaluation.
+#include "common.cuh"
+#include "kernels.h"
+
+namespace acu {
+
+// ---------------------------------------------------------------------------
+// Backprojection: tomography/tv_hpc.F90:107-123.
+//   img(jx,jy) = cmask(jx,jy) * sum_theta [ q(y1)*(y2-yr) + q(y2)*(yr-y1) ]
+//   yr = sin(c)*(jx-m) + cos(c)*(jy-m) + m,  c = pi*(90-theta)/180,
+//   taps used only when y1 = floor(yr) > 1 and y2 = y1+1 < N+1.
+// One thread per pixel and slice group; angles summed in the reference's
+// order.  Pixels whose mask is zero are written as 0 without the angle loop.
+// ---------------------------------------------------------------------------
+template <typename Real, int V>
+__global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
+                                                     const Real* __restrict__ cmask,
+                                                     const Real* __restrict__ sc, Real* __restrict__ img,
+                                                     int N, int T, Real mid)
+{
+    const int jx = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int jy = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int g = blockIdx.z;
+    if (jx > N || jy > N) return;
+    const size_t pix = (size_t)(jy - 1) * N + (jx - 1);
+    const Real cm = cmask[pix];
+    Lanes<Real, V> acc;
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = Real(0);
+    if (cm != Real(0)) {
+        const Real dx = (Real)jx - mid, dy = (Real)jy - mid;
+        const Real* qg = q + (size_t)g * T * N * V;
+        for (int t = 0; t < T; ++t) {
+            const Lanes<Real, 2> scp = ld_lanes<Real, 2>(sc + 2 * t);
+            const Real s = scp.v[0], c = scp.v[1];
+            const Real yr = add_rn(add_rn(mul_rn(s, dx), mul_rn(c, dy)), mid);
+            const Real y1f = rfloor(yr);
+            const int y1 = (int)y1f;
+            if (y1 > 1 && y1 < N) {
+                const Real wl = add_rn(y1f, Real(1)) - yr;
+                const Real wh = yr - y1f;
+                const Real* row = qg + ((size_t)t * N + (y1 - 1)) * V;
+                const Lanes<Real, V> a = ld_lanes<Real, V>(row);
+                const Lanes<Real, V> b = ld_lanes<Real, V>(row + V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc.v[v] = fma(b.v[v], wh, fma(a.v[v], wl, acc.v[v]));
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = cm * acc.v[v];
+    st_lanes<Real, V>(img + ((size_t)g * N * N + pix) * V, acc);
+}
+
+template <typename Real, int V>
+void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st)
+{
+    dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G);
+    k_backproject<Real, V><<<grd, blk, 0, st>>>(q, g.cmask, g.sc_bp, img, g.N, g.T, g.mid);
+}
+
+// ---------------------------------------------------------------------------
+// Projector: tomography/tv_hpc.F90:137-156.
+//   sino(jy,theta) = (1/N) sum_jx bilinear(img; xr, yr)
+//   xr = cos(c)*(jx-m) - sin(c)*(jy-m) + m, yr = sin(c)*(jx-m) + cos(c)*(jy-m) + m,
+//   c = pi*(theta-90)/180; a sample counts when min(x1,y1) > 1 and
+//   max(x1+1,y1+1) < N+1.
+// One thread per (bin, angle) ray and slice group, steps in the reference's
+// order.  The four bilinear weights are formed once per sample and shared by
+// the V slices.
+// ---------------------------------------------------------------------------
+template <typename Real, int V>
+__global__ void __launch_bounds__(128) k_radon(const Real* __restrict__ img, const Real* __restrict__ sc,
+                                               Real* __restrict__ sino, int N, int T, Real mid)
+{
+    const int jy = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int t = blockIdx.y * blockDim.y + threadIdx.y;
+    const int g = blockIdx.z;
+    if (jy > N || t >= T) return;
+    const Real s = sc[2 * t], c = sc[2 * t + 1];
+    const Real dyv = (Real)jy - mid;
+    const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+    const Real* u = img + (size_t)g * N * N * V;
+    const size_t rowstride = (size_t)N * V;
+    Lanes<Real, V> acc;
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = Real(0);
+    for (int jx = 1; jx <= N; ++jx) {
+        const Real dxv = (Real)jx - mid;
+        const Real xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
+        const Real yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
+        const Real x1f = rfloor(xr), y1f = rfloor(yr);
+        const int x1 = (int)x1f, y1 = (int)y1f;
+        if (min(x1, y1) > 1 && max(x1, y1) < N) {
+            const Real wxl = add_rn(x1f, Real(1)) - xr, wxh = xr - x1f;
+            const Real wyl = add_rn(y1f, Real(1)) - yr, wyh = yr - y1f;
+            const Real w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
+            const Real* p = u + ((size_t)(y1 - 1) * N + (x1 - 1)) * V;
+            const Lanes<Real, V> a = ld_lanes<Real, V>(p);
+            const Lanes<Real, V> b = ld_lanes<Real, V>(p + V);
+            const Lanes<Real, V> cc = ld_lanes<Real, V>(p + rowstride);
+            const Lanes<Real, V> d = ld_lanes<Real, V>(p + rowstride + V);
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                acc.v[v] = fma(d.v[v], w22, fma(cc.v[v], w12, fma(b.v[v], w21, fma(a.v[v], w11, acc.v[v]))));
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = acc.v[v] / (Real)N;
+    st_lanes<Real, V>(sino + (((size_t)g * T + t) * N + (jy - 1)) * V, acc);
+}
+
+template <typename Real, int V>
+void launch_radon(const DevGeom<Real>& g, int G, const Real* img, Real* sino, cudaStream_t st)
+{
+    dim3 blk(32, 4), grd((g.N + 31) / 32, (g.T + 3) / 4, G);
+    k_radon<Real, V><<<grd, blk, 0, st>>>(img, g.sc_fp, sino, g.N, g.T, g.mid);
+}
+
+// ---------------------------------------------------------------------------
+// Exact transpose of k_radon, as a gather (no atomics, deterministic).  For
+// pixel (px,py) and angle theta the samples that use it as a bilinear tap lie
+// within sqrt(2) of its inverse-rotated position; each candidate sample is
+// re-evaluated with the projector's own arithmetic, so cells and weights are
+// identical to the forward operator's.
+// ---------------------------------------------------------------------------
+template <typename Real, int V>
+__global__ void __launch_bounds__(256) k_radon_adjoint(const Real* __restrict__ sino,
+                                                       const Real* __restrict__ sc,
+                                                       Real* __restrict__ img, int N, int T, Real mid)
+{
+    const int px = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int py = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int g = blockIdx.z;
+    if (px > N || py > N) return;
+    Lanes<Real, V> acc;
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = Real(0);
+    // A pixel on the border is never a tap (taps span 2..N).
+    if (px >= 2 && py >= 2) {
+        const Real* yg = sino + (size_t)g * T * N * V;
+        const Real ex = (Real)px - mid, ey = (Real)py - mid;
+        for (int t = 0; t < T; ++t) {
+            const Lanes<Real, 2> scp = ld_lanes<Real, 2>(sc + 2 * t);
+            const Real s = scp.v[0], c = scp.v[1];
+            // tap (px,py) of a sample at (xr,yr) means xr in [px-1,px+1), yr in [py-1,py+1)
+            const Real u = c * ex + s * ey + mid;       // jx of the sample at the pixel
+            const Real w = -s * ex + c * ey + mid;      // jy
+            int jx0 = (int)rfloor(u - Real(1.5)), jx1 = (int)rfloor(u + Real(1.5)) + 1;
+            int jy0 = (int)rfloor(w - Real(1.5)), jy1 = (int)rfloor(w + Real(1.5)) + 1;
+            jx0 = max(jx0, 1); jy0 = max(jy0, 1); jx1 = min(jx1, N); jy1 = min(jy1, N);
+            const Real* yt = yg + (size_t)t * N * V;
+            for (int jy = jy0; jy <= jy1; ++jy) {
+                const Real dyv = (Real)jy - mid;
+                const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+                Real wsum = Real(0);
+                for (int jx = jx0; jx <= jx1; ++jx) {
+                    const Real dxv = (Real)jx - mid;
+                    const Real xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
+                    const Real yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
+                    const Real x1f = rfloor(xr), y1f = rfloor(yr);
+                    const int x1 = (int)x1f, y1 = (int)y1f;
+                    if (min(x1, y1) > 1 && max(x1, y1) < N && (px == x1 || px == x1 + 1) &&
+                        (py == y1 || py == y1 + 1)) {
+                        const Real wx = (px == x1) ? (add_rn(x1f, Real(1)) - xr) : (xr - x1f);
+                        const Real wy = (py == y1) ? (add_rn(y1f, Real(1)) - yr) : (yr - y1f);
+                        wsum += wx * wy;
+                    }
+                }
+                if (wsum != Real(0)) {
+                    const Lanes<Real, V> yv = ld_lanes<Real, V>(yt + (size_t)(jy - 1) * V);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc.v[v] = fma(wsum, yv.v[v], acc.v[v]);
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = acc.v[v] / (Real)N;
+    st_lanes<Real, V>(img + ((size_t)g * N * N + (size_t)(py - 1) * N + (px - 1)) * V, acc);
+}
+
+template <typename Real, int V>
+void launch_radon_adjoint(const DevGeom<Real>& g, int G, const Real* sino, Real* img, cudaStream_t st)
+{
+    dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G);
+    k_radon_adjoint<Real, V><<<grd, blk, 0, st>>>(sino, g.sc_fp, img, g.N, g.T, g.mid);
+}
+
+// ---------------------------------------------------------------------------
+// Direct ramp filter: tomography/tv_hpc.F90:93-105.
+//   out(i,theta) = sum_{j=1..N} sino(j,theta) * filter(i - j + N + 1)
+// (every tap lies inside the 2N+1 table).  One block per (angle, group); the
+// row and the taps are staged in shared memory; each thread accumulates
+// RB consecutive outputs so every row value loaded is used RB times.
+// ---------------------------------------------------------------------------
+template <typename Real, int V, int RB>
+__global__ void __launch_bounds__(256) k_filter_direct(const Real* __restrict__ sino,
+                                                       const Real* __restrict__ filt,
+                                                       Real* __restrict__ out, int N, int T)
+{
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Real* s_x = reinterpret_cast<Real*>(smem_raw);   // N*V
+    Real* s_h = s_x + (size_t)N * V;                 // 2N+1
+    const int t = blockIdx.x, g = blockIdx.y;
+    const Real* row = sino + ((size_t)g * T + t) * N * V;
+    for (int i = threadIdx.x; i < N * V; i += blockDim.x) s_x[i] = row[i];
+    for (int i = threadIdx.x; i < 2 * N + 1; i += blockDim.x) s_h[i] = filt[i];
+    __syncthreads();
+    Real* orow = out + ((size_t)g * T + t) * N * V;
+    for (int i0 = threadIdx.x * RB; i0 < N; i0 += blockDim.x * RB) {
+        Lanes<Real, V> acc[RB];
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+#pragma unroll
+            for (int v = 0; v < V; ++v) acc[r].v[v] = Real(0);
+        // output i uses tap index i - j + N (0-based i, j)
+        for (int j = 0; j < N; ++j) {
+            Lanes<Real, V> x;
+#pragma unroll
+            for (int v = 0; v < V; ++v) x.v[v] = s_x[(size_t)j * V + v];
+#pragma unroll
+            for (int r = 0; r < RB; ++r) {
+                const Real h = s_h[i0 + r - j + N];
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc[r].v[v] = fma(x.v[v], h, acc[r].v[v]);
+            }
+        }
+#pragma unroll
+        for (int r = 0; r < RB; ++r)
+            if (i0 + r < N) st_lanes<Real, V>(orow + (size_t)(i0 + r) * V, acc[r]);
+    }
+}
+
+template <typename Real, int V>
+void launch_filter_direct(const DevGeom<Real>& g, int G, const Real* sino, Real* out, cudaStream_t st)
+{
+    constexpr int RB = 4;
+    size_t sm = sizeof(Real) * ((size_t)g.N * V + 2 * (size_t)g.N + 1 + RB);
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaFuncSetAttribute(k_filter_direct<Real, V, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             227 * 1024);
+        attr_set = true;
+    }
+    dim3 grd(g.T, G);
+    k_filter_direct<Real, V, RB><<<grd, 256, sm, st>>>(sino, g.filt, out, g.N, g.T);
+}
+
+// ---- explicit instantiations ------------------------------------------------
+#define ACU_INST(R, V)                                                                          \
+    template void launch_backproject<R, V>(const DevGeom<R>&, int, const R*, R*, cudaStream_t);  \
+    template void launch_radon<R, V>(const DevGeom<R>&, int, const R*, R*, cudaStream_t);       \
+    template void launch_radon_adjoint<R, V>(const DevGeom<R>&, int, const R*, R*, cudaStream_t); \
+    template void launch_filter_direct<R, V>(const DevGeom<R>&, int, const R*, R*, cudaStream_t);
+ACU_INST(float, 1)
+ACU_INST(float, 4)
+ACU_INST(double, 1)
+#undef ACU_INST
+
+}  // namespace acu

@@ -1,0 +1,105 @@
+// Host-side geometry tables of one reconstruction grid (int_radon,
+// tomography/tv_hpc.F90:11-78) in single or double precision.
+//
+// Built with -ffp-contract=off so that single precision is evaluated in the
+// reference's operation order with the C library's sinf/cosf/expf/sqrtf; the
+// tables are uploaded once and every kernel reads them, so the mask, the
+// filter taps and the per-angle sines are identical to the reference's.
+#include "tables.h"
+
+#include <cmath>
+#include <complex>
+
+namespace acu {
+
+template <typename Real>
+static Real r_atan(Real x) { return std::atan(x); }
+template <typename Real>
+static Real r_sin(Real x) { return std::sin(x); }
+template <typename Real>
+static Real r_cos(Real x) { return std::cos(x); }
+template <typename Real>
+static Real r_exp(Real x) { return std::exp(x); }
+template <typename Real>
+static Real r_sqrt(Real x) { return std::sqrt(x); }
+
+template <typename Real>
+void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& out)
+{
+    const Real pi = Real(4) * r_atan<Real>(Real(1));
+    out.N = N;
+    out.T = T;
+    out.mid = (Real)((N + 1) / 2);
+    // filter taps, tv_hpc.F90:53-56
+    out.filt.resize(2 * (size_t)N + 1);
+    for (int jx = 1; jx <= 2 * N + 1; ++jx) {
+        long k = (long)(jx - 1 - N);
+        long den = 4 * k * k - 1;
+        out.filt[jx - 1] = -((Real(2) * (Real)N) / ((pi * pi) * (Real)den));
+    }
+    // mask, tv_hpc.F90:58-74
+    out.cmask.resize((size_t)N * N);
+    const Real rad_n = (Real)(N - 1) / Real(2) - (Real)wpu;
+    for (int jy = 1; jy <= N; ++jy) {
+        for (int jx = 1; jx <= N; ++jx) {
+            Real ax = ((Real)jx - ((Real)N - Real(1)) / Real(2)) - Real(1);
+            Real ay = ((Real)jy - ((Real)N - Real(1)) / Real(2)) - Real(1);
+            Real rr = r_sqrt<Real>(ax * ax + ay * ay);
+            Real rtmp = Real(1) - (Real(2) * (rr - rad_n)) / (Real)wpu;
+            Real v;
+            if (rtmp <= Real(0)) {
+                v = Real(0);
+            } else if (rtmp >= Real(1)) {
+                v = pi / (Real)T;
+            } else {
+                Real in = r_exp<Real>(Real(1) - Real(1) / (Real(1) - rtmp));
+                v = (pi * r_exp<Real>(Real(1) - Real(1) / (Real(1) - in))) / (Real)T;
+            }
+            out.cmask[(size_t)(jy - 1) * N + (jx - 1)] = v;
+        }
+    }
+    // angle tables, tv_hpc.F90:113 and :142
+    out.sc_bp.resize(2 * (size_t)T);
+    out.sc_fp.resize(2 * (size_t)T);
+    for (int t = 0; t < T; ++t) {
+        Real th = (Real)theta[t];
+        Real ctb = (pi * (Real(90) - th)) / Real(180);
+        Real ctf = (pi * (th - Real(90))) / Real(180);
+        out.sc_bp[2 * t] = r_sin<Real>(ctb);
+        out.sc_bp[2 * t + 1] = r_cos<Real>(ctb);
+        out.sc_fp[2 * t] = r_sin<Real>(ctf);
+        out.sc_fp[2 * t + 1] = r_cos<Real>(ctf);
+    }
+    // FFT form of the same filter: circular kernel of length L >= 2N-2 holding
+    // taps -(N-1)..(N-1) (the two taps +-(N-1) are equal and share one slot
+    // when L = 2N-2); its DFT is real because the kernel is symmetric.
+    int L = 1, lg = 0;
+    while (L < 2 * N - 2) { L <<= 1; ++lg; }
+    if (L < 16) { L = 16; lg = 4; }
+    out.fft_L = L;
+    out.fft_log2L = lg;
+    std::vector<double> c(L, 0.0);
+    const double pid = 4.0 * std::atan(1.0);
+    for (int k = -(N - 1); k <= N - 1; ++k) c[((k % L) + L) % L] = (double)out.filt[k + N];
+    // fft_h = DFT(c) / L (the inverse transform's 1/L folded in), in double
+    std::vector<double> cosj(L);
+    for (int j = 0; j < L; ++j) cosj[j] = std::cos(2.0 * pid * (double)j / (double)L);
+    out.fft_h.resize(L);
+    for (int m = 0; m < L; ++m) {
+        long double acc = c[0];
+        for (int k = 1; k < L / 2; ++k) acc += 2.0L * (long double)c[k] * (long double)cosj[((long)k * m) % L];
+        acc += (long double)c[L / 2] * ((m % 2) ? -1.0L : 1.0L);
+        out.fft_h[m] = (Real)(acc / (long double)L);
+    }
+    out.fft_tw.resize(2 * (size_t)L);   // (cos, sin) of -2 pi k / L, k < L
+    for (int k = 0; k < L; ++k) {
+        double a = -2.0 * pid * (double)k / (double)L;
+        out.fft_tw[2 * k] = std::cos(a);
+        out.fft_tw[2 * k + 1] = std::sin(a);
+    }
+}
+
+template void make_tables<float>(int, int, const float*, int, HostTables<float>&);
+template void make_tables<double>(int, int, const float*, int, HostTables<double>&);
+
+}  // namespace acu

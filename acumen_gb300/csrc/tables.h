@@ -1,0 +1,23 @@
+// Host geometry tables (see tables.cpp).
+#pragma once
+#include <vector>
+
+namespace acu {
+
+template <typename Real>
+struct HostTables {
+    int N = 0, T = 0;
+    Real mid = 0;
+    std::vector<Real> filt;    // 2N+1
+    std::vector<Real> cmask;   // N*N
+    std::vector<Real> sc_bp;   // 2T
+    std::vector<Real> sc_fp;   // 2T
+    std::vector<Real> fft_h;   // L
+    std::vector<double> fft_tw;  // 2*L: cos, sin of -2 pi k / L
+    int fft_L = 0, fft_log2L = 0;
+};
+
+template <typename Real>
+void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& out);
+
+}  // namespace acu

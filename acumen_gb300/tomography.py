@@ -1,0 +1,186 @@
+"""Python mirror of the reference's Fortran module ``Tomography``
+(tomography/tv_hpc.F90:1-390) on top of the C ABI.
+
+=====================  ====================================================
+reference               here
+=====================  ====================================================
+int_radon()             ``Tomography(nimage, theta, wpu)``  (tv_hpc.F90:11)
+radon(sino, img)        ``t.radon(img)``                    (:129)
+iradon(img, sino)       ``t.iradon(sino)``                  (:84)
+tvopt(tv, fbp, slice)   ``t.tvopt(f, ninner, nouter, ncg, lam, mu)`` (:162)
+get_slice(fbp)          ``t.get_slice(f)``                  (:365)
+fin_radon()             ``t.close()``                       (:80)
+=====================  ====================================================
+
+Arrays use the Fortran storage order of the reference with the first index
+fastest: ``img[..., jy-1, jx-1]``, ``sino[..., jtheta-1, jbin-1]``; leading
+axes are slices.  numpy arrays go through the host-buffer entry points;
+CUDA torch tensors go through the ``_dev`` entry points on torch's current
+stream (float64 tensors through the ``_f64`` variants).  The module state of
+the reference (ncg, nouter, lambda, mu, wpu, ...) becomes call arguments.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from ._lib import call, check, lib
+
+try:  # torch is optional for the host-buffer path
+    import torch
+except Exception:  # pragma: no cover
+    torch = None
+
+
+def _is_cuda_tensor(x):
+    return torch is not None and isinstance(x, torch.Tensor) and x.is_cuda
+
+
+class Tomography:
+    def __init__(self, nimage: int, theta, wpu: int):
+        th = np.ascontiguousarray(np.asarray(theta, dtype=np.float32))
+        self.nimage = int(nimage)
+        self.ntheta = int(th.size)
+        self.wpu = int(wpu)
+        self.theta = th
+        h = ctypes.c_void_p()
+        call("acu_ctx_create", ctypes.byref(h), self.nimage, self.ntheta,
+             th.ctypes.data_as(ctypes.c_void_p), self.wpu)
+        self._h = h
+
+    # -- lifecycle --------------------------------------------------------------
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().acu_ctx_destroy(self._h)
+            self._h = None
+
+    fin_radon = close
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    @property
+    def handle(self):
+        return self._h
+
+    def set_option(self, option: int, value: int):
+        call("acu_set_option", self._h, int(option), int(value), ctx=self._h)
+
+    def get_option(self, option: int) -> int:
+        v = ctypes.c_int()
+        call("acu_get_option", self._h, int(option), ctypes.byref(v), ctx=self._h)
+        return v.value
+
+    def _sync_stream(self):
+        if torch is not None and torch.cuda.is_available():
+            call("acu_set_stream", self._h, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream),
+                 ctx=self._h)
+
+    # -- helpers -------------------------------------------------------------------
+    def _shape_in(self, x, kind):
+        N, T = self.nimage, self.ntheta
+        tail = (T, N) if kind == "sino" else (N, N)
+        if tuple(x.shape[-2:]) != tail:
+            raise ValueError(f"expected trailing shape {tail} ({kind}), got {tuple(x.shape)}")
+        lead = tuple(x.shape[:-2])
+        S = int(np.prod(lead)) if lead else 1
+        return lead, S
+
+    def _op(self, name, x, kin, kout):
+        lead, S = self._shape_in(x, kin)
+        N, T = self.nimage, self.ntheta
+        tail = (T, N) if kout == "sino" else (N, N)
+        if _is_cuda_tensor(x):
+            if x.dtype == torch.float64:
+                fn = name + "_dev_f64"
+            elif x.dtype == torch.float32:
+                fn = name + "_dev"
+            else:
+                raise TypeError("CUDA tensors must be float32 or float64")
+            x = x.contiguous()
+            out = torch.empty(lead + tail, dtype=x.dtype, device=x.device)
+            self._sync_stream()
+            call(fn, self._h, S, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(out.data_ptr()), ctx=self._h)
+            return out
+        a = np.ascontiguousarray(np.asarray(x, dtype=np.float32))
+        out = np.empty(lead + tail, np.float32)
+        call(name, self._h, S, a.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p),
+             ctx=self._h)
+        return out
+
+    # -- the module's subroutines --------------------------------------------------
+    def radon(self, img):
+        """tomography/tv_hpc.F90:129-159."""
+        return self._op("acu_radon", img, "img", "sino")
+
+    def iradon(self, sino):
+        """tomography/tv_hpc.F90:84-126 (filter, backprojection, mask)."""
+        return self._op("acu_iradon", sino, "sino", "img")
+
+    get_slice = iradon  # tomography/tv_hpc.F90:365-386: iradon with copies
+
+    def radon_adjoint(self, sino):
+        """Exact transpose of radon (not in the reference)."""
+        return self._op("acu_radon_adjoint", sino, "sino", "img")
+
+    def filter(self, sino):
+        """First half of iradon: the ramp filter (tv_hpc.F90:93-105); CUDA tensors only."""
+        lead, S = self._shape_in(sino, "sino")
+        out = torch.empty_like(sino)
+        self._sync_stream()
+        call("acu_filter_dev", self._h, S, ctypes.c_void_p(sino.data_ptr()), ctypes.c_void_p(out.data_ptr()),
+             ctx=self._h)
+        return out
+
+    def backproject(self, filtered):
+        """Second half of iradon (tv_hpc.F90:107-123); CUDA tensors only."""
+        lead, S = self._shape_in(filtered, "sino")
+        out = torch.empty(lead + (self.nimage, self.nimage), dtype=filtered.dtype, device=filtered.device)
+        self._sync_stream()
+        call("acu_backproject_dev", self._h, S, ctypes.c_void_p(filtered.data_ptr()),
+             ctypes.c_void_p(out.data_ptr()), ctx=self._h)
+        return out
+
+    def tvopt(self, f, ninner: int, nouter: int, ncg: int, lam: float, mu: float, plain: bool = False):
+        """tomography/tv_hpc.F90:162-363: returns (tv, fbp).  plain=True runs
+        the per-slice reference-structured GPU path."""
+        lead, S = self._shape_in(f, "sino")
+        N = self.nimage
+        if _is_cuda_tensor(f):
+            f = f.contiguous()
+            tv = torch.empty(lead + (N, N), dtype=f.dtype, device=f.device)
+            fbp = torch.empty_like(tv)
+            if f.dtype == torch.float64:
+                if plain:
+                    raise ValueError("the per-slice path is single precision")
+                fn = "acu_tvopt_dev_f64"
+            else:
+                fn = "acu_tvopt_plain_dev" if plain else "acu_tvopt_dev"
+            self._sync_stream()
+            conv = float
+            call(fn, self._h, S, ctypes.c_void_p(f.data_ptr()), int(ninner), int(nouter), int(ncg), conv(lam),
+                 conv(mu), ctypes.c_void_p(tv.data_ptr()), ctypes.c_void_p(fbp.data_ptr()), ctx=self._h)
+            return tv, fbp
+        a = np.ascontiguousarray(np.asarray(f, dtype=np.float32))
+        tv = np.empty(lead + (N, N), np.float32)
+        fbp = np.empty_like(tv)
+        call("acu_tvopt_plain" if plain else "acu_tvopt", self._h, S, a.ctypes.data_as(ctypes.c_void_p),
+             int(ninner), int(nouter), int(ncg), float(lam), float(mu), tv.ctypes.data_as(ctypes.c_void_p),
+             fbp.ctypes.data_as(ctypes.c_void_p), ctx=self._h)
+        return tv, fbp
+
+    def last_delta(self, nslices: int):
+        out = np.zeros(nslices, np.float64)
+        call("acu_tv_last_delta", self._h, int(nslices), out.ctypes.data_as(ctypes.c_void_p), ctx=self._h)
+        return out

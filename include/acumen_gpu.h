@@ -1,0 +1,117 @@
+/*
+ * acumen_gpu.h -- C ABI of the GB300 tomography library (libacumen_gpu.so).
+ *
+ * Drop-in replacement for the compute of the reference's Fortran module
+ * `Tomography` (tomography/tv_hpc.F90:1-390) and of the inline kernels of
+ * tomography/projections_to_sinogram_hpc.F90 and tomography/fits_to_hpc.F90.
+ * The reference exposes no C interface: its callers are the Fortran driver
+ * programs, which bind these entry points through ISO_C_BINDING (the
+ * interface module is acumen_gb300/fortran/acumen_gpu.f90).
+ *
+ * Conventions
+ *  - Every function returns int: ACU_OK (0) or a negative ACU_ERR_* code;
+ *    acu_last_error(ctx) gives the message (acu_last_error(NULL) for errors
+ *    raised before a context exists).  Nothing aborts the process.
+ *  - Arrays are single precision in the reference's Fortran order, first index
+ *    fastest: image img(jx,jy) is N*N floats with x fastest; sinogram
+ *    sino(jbin,jtheta) is T*N floats with the bin fastest; S slices are
+ *    stored one after another.  Angles are degrees, as in theta.dat.
+ *  - Functions without a suffix take HOST pointers: they copy in, compute and
+ *    copy out, and return when the results are in host memory.  The `_dev`
+ *    variants take DEVICE pointers, are ordered on the context's stream and
+ *    do not synchronise.  `_f64` variants run the same kernels in double
+ *    precision on double arrays (used to check the single-precision path).
+ *  - A context is used by one host thread at a time; contexts are
+ *    independent.  The library owns its device work buffers.
+ */
+#ifndef ACUMEN_GPU_H
+#define ACUMEN_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define ACU_OK 0
+#define ACU_ERR_INVALID (-1)     /* bad argument (size, pointer, mode) */
+#define ACU_ERR_CUDA (-2)        /* a CUDA runtime call failed */
+#define ACU_ERR_NOMEM (-3)       /* device or host allocation failed */
+#define ACU_ERR_TIMEOUT (-4)     /* a bounded device wait gave up */
+#define ACU_ERR_UNSUPPORTED (-5) /* valid request this build does not handle */
+
+typedef struct acu_ctx acu_ctx;
+
+/* ---- context: tomography/tv_hpc.F90:11-82 (int_radon / fin_radon) ---------
+ * Creates the geometry of one reconstruction grid: nimage = N (the grid side,
+ * equal to the number of detector bins), ntheta = T angles theta_deg[T],
+ * taper width wpu of the circular mask.  Computes the filter taps and mask
+ * (int_radon, tv_hpc.F90:53-74).  nimage = 0 creates a context without a
+ * grid, for the preprocessing functions only.                               */
+int acu_ctx_create(acu_ctx **ctx, int nimage, int ntheta, const float *theta_deg, int wpu);
+/* tv_hpc.F90:80-82 (fin_radon): releases every device buffer of ctx. */
+int acu_ctx_destroy(acu_ctx *ctx);
+const char *acu_last_error(const acu_ctx *ctx);
+/* Orders all later work of ctx on this cudaStream_t; NULL (the default) is the
+ * legacy default stream.  CUDA graphs are captured on a private stream and
+ * launched on this one. */
+int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
+
+#define ACU_OPT_FILTER 1    /* 0: FFT ramp filter (default); 1: direct O(N^2) sum (tv_hpc.F90:93-105) */
+#define ACU_OPT_LANES 2     /* slices per thread in batched kernels: 0 auto (default), 1 or 4 */
+#define ACU_OPT_GRAPH 3     /* 1: capture the Bregman outer iteration as a CUDA graph (default); 0: launch */
+#define ACU_OPT_VERBOSE 4   /* 1: print the reference's "Slice/Loop/delta" lines (tv_hpc.F90:350-352) */
+#define ACU_OPT_PRINT_EVERY 5 /* outer-loop period of those lines: 50 (tv_hpc) or 10 (tv_hpc_slice) */
+int acu_set_option(acu_ctx *ctx, int option, int value);
+int acu_get_option(const acu_ctx *ctx, int option, int *value);
+
+/* ---- Radon operators -------------------------------------------------------
+ * acu_iradon: tomography/tv_hpc.F90:84-126 (iradon) -- ramp filter along each
+ *   sinogram column, pixel-driven linear-interpolation backprojection, times
+ *   the tapered mask.  sino: S*T*N, img: S*N*N.  Also get_slice
+ *   (tv_hpc.F90:365-386, fbp_hpc.F90:129-150), which is iradon with copies.
+ * acu_radon: tomography/tv_hpc.F90:129-159 (radon) -- bilinear ray sums / N.
+ * acu_radon_adjoint: exact transpose of acu_radon (new; not in the reference):
+ *   <radon(x), y> = <x, radon_adjoint(y)> up to round-off.
+ * acu_filter_dev / acu_backproject_dev: the two halves of iradon
+ *   (tv_hpc.F90:93-105 and :107-123).                                         */
+int acu_iradon(acu_ctx *ctx, int nslices, const float *sino, float *img);
+int acu_radon(acu_ctx *ctx, int nslices, const float *img, float *sino);
+int acu_radon_adjoint(acu_ctx *ctx, int nslices, const float *sino, float *img);
+int acu_iradon_dev(acu_ctx *ctx, int nslices, const float *d_sino, float *d_img);
+int acu_radon_dev(acu_ctx *ctx, int nslices, const float *d_img, float *d_sino);
+int acu_radon_adjoint_dev(acu_ctx *ctx, int nslices, const float *d_sino, float *d_img);
+int acu_filter_dev(acu_ctx *ctx, int nslices, const float *d_sino, float *d_out);
+int acu_backproject_dev(acu_ctx *ctx, int nslices, const float *d_filtered, float *d_img);
+int acu_iradon_dev_f64(acu_ctx *ctx, int nslices, const double *d_sino, double *d_img);
+int acu_radon_dev_f64(acu_ctx *ctx, int nslices, const double *d_img, double *d_sino);
+int acu_radon_adjoint_dev_f64(acu_ctx *ctx, int nslices, const double *d_sino, double *d_img);
+
+/* ---- split-Bregman TV: tomography/tv_hpc.F90:162-363 (tvopt) ---------------
+ * Solves every slice of f (S*T*N) with ninner x nouter Bregman iterations of
+ * ncg CG steps each; writes the TV result to tv_out and the FBP warm start to
+ * fbp_out (S*N*N each; fbp_out may be NULL).  Batched: all S slices advance
+ * together, CG inner products / step lengths / residual norms in FP64 on the
+ * device, the outer iteration replayed as a CUDA graph.
+ * acu_tvopt_plain*: the same algorithm as one slice at a time with one kernel
+ *   per loop of the reference, direct filter, and the CG scalars read back to
+ *   the host every step, as the reference does (the per-slice comparator).  */
+int acu_tvopt(acu_ctx *ctx, int nslices, const float *f, int ninner, int nouter, int ncg,
+              float lambda, float mu, float *tv_out, float *fbp_out);
+int acu_tvopt_dev(acu_ctx *ctx, int nslices, const float *d_f, int ninner, int nouter, int ncg,
+                  float lambda, float mu, float *d_tv, float *d_fbp);
+int acu_tvopt_plain(acu_ctx *ctx, int nslices, const float *f, int ninner, int nouter, int ncg,
+                    float lambda, float mu, float *tv_out, float *fbp_out);
+int acu_tvopt_plain_dev(acu_ctx *ctx, int nslices, const float *d_f, int ninner, int nouter,
+                        int ncg, float lambda, float mu, float *d_tv, float *d_fbp);
+int acu_tvopt_dev_f64(acu_ctx *ctx, int nslices, const double *d_f, int ninner, int nouter,
+                      int ncg, double lambda, double mu, double *d_tv, double *d_fbp);
+/* Print-only Err_diff of the last outer iteration per slice (tv_hpc.F90:327-333),
+ * available after a tvopt call with ACU_OPT_VERBOSE set.                     */
+int acu_tv_last_delta(const acu_ctx *ctx, int nslices, double *delta);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ACUMEN_GPU_H */

@@ -1,0 +1,52 @@
+"""CPU checks of the C ABI: the library builds, loads without a GPU, exports
+every entry point include/*.h declares, and rejects bad arguments before
+touching the device."""
+import ctypes
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = []
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        txt = open(h).read()
+        names += re.findall(r"^\s*(?:int|const char \*|const char\*)\s*\*?\s*(acu_\w+)\s*\(", txt, re.M)
+    return sorted(set(names))
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("acu_ctx_create", "acu_iradon", "acu_radon", "acu_tvopt", "acu_radon_adjoint"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    L = ctypes.CDLL(built_lib)
+    missing = [n for n in declared_functions() if not hasattr(L, n)]
+    assert not missing, missing
+
+
+def test_invalid_geometry_rejected_without_gpu(built_lib):
+    from acumen_gb300 import _lib
+    L = _lib.lib()
+    h = ctypes.c_void_p()
+    rc = L.acu_ctx_create(ctypes.byref(h), 2, 10, None, 4)
+    assert rc == _lib.ACU_ERR_INVALID
+    assert b"invalid geometry" in L.acu_last_error(None)
+    rc = L.acu_ctx_create(None, 65, 10, None, 4)
+    assert rc == _lib.ACU_ERR_INVALID
+    assert L.acu_set_option(None, 1, 0) == _lib.ACU_ERR_INVALID
+
+
+def test_python_mirror_raises_on_missing_library(tmp_path, monkeypatch):
+    from acumen_gb300 import _lib
+    monkeypatch.setattr(_lib, "LIB_PATH", str(tmp_path / "nope.so"))
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        _lib.lib()

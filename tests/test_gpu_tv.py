@@ -1,0 +1,111 @@
+"""GPU parity of the split-Bregman TV solver (tomography/tv_hpc.F90:162-363).
+
+Tolerance: relative L2 <= 1e-4 against the FP64 oracle after the fixed
+iteration count, measured inside the reconstruction disc (mask > 0).  Outside
+the disc the reference's normal operator reduces to lambda times the periodic
+Laplacian (iradon is masked there), which is nearly singular; there the
+oracle's own single-precision run departs from its FP64 run by O(1e-4), so
+the full-image figure is checked against a looser bound and reported.
+The double-precision GPU solver matches the FP64 oracle to 1e-9.
+"""
+import numpy as np
+import pytest
+import torch
+
+from acumen_gb300 import synthetic as syn
+from acumen_gb300.tomography import Tomography
+
+pytestmark = pytest.mark.gpu
+
+TV_TOL = 1e-4
+
+
+def rel(a, b, mask=None):
+    a = np.asarray(a.cpu() if isinstance(a, torch.Tensor) else a, np.float64)
+    b = np.asarray(b.cpu() if isinstance(b, torch.Tensor) else b, np.float64)
+    if mask is not None:
+        a, b = a[..., mask], b[..., mask]
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def prob(built_lib, oracle):
+    N, T, wpu = 65, 60, 6
+    th = syn.angles(T)
+    f = np.stack([syn.normalised_sinogram(syn.random_ellipses(s, 0.3 * N), N, th, I0=5e3, seed=s).numpy()
+                  for s in range(5)])
+    args = dict(ninner=1, nouter=8, ncg=5, lam=0.05, mu=1.0)
+    ref = [oracle.tvopt(f[s].astype(np.float64), th, wpu, args["ninner"], args["nouter"], args["ncg"],
+                        args["lam"], args["mu"], prec=64) for s in range(5)]
+    tv64 = np.stack([r[0] for r in ref])
+    fbp64 = np.stack([r[1] for r in ref])
+    mask = oracle.cmask(N, T, wpu, 64) > 0
+    return dict(N=N, T=T, wpu=wpu, th=th, f=f, args=args, tv64=tv64, fbp64=fbp64, mask=mask)
+
+
+@pytest.mark.parametrize("S", [1, 5])
+def test_batched_tv_matches_fp64_oracle(prob, S):
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    a = prob["args"]
+    tv, fbp = t.tvopt(torch.from_numpy(prob["f"][:S]).cuda(), a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    assert rel(fbp, prob["fbp64"][:S]) < 1e-5
+    assert rel(tv, prob["tv64"][:S], prob["mask"]) < TV_TOL
+    assert rel(tv, prob["tv64"][:S]) < 2e-3
+
+
+def test_plain_path_matches_batched(prob):
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    a = prob["args"]
+    f = torch.from_numpy(prob["f"][:3]).cuda()
+    tvp, fbpp = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"], plain=True)
+    assert rel(tvp, prob["tv64"][:3], prob["mask"]) < TV_TOL
+    assert rel(fbpp, prob["fbp64"][:3]) < 1e-5
+
+
+def test_graph_replay_equals_launches(prob):
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    a = prob["args"]
+    f = torch.from_numpy(prob["f"][:4]).cuda()
+    tv_g, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    t.set_option(3, 0)
+    tv_l, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    torch.testing.assert_close(tv_g, tv_l, rtol=0, atol=0)
+
+
+def test_host_entry_point_and_ninner(prob, oracle):
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    f = prob["f"][:2].astype(np.float32)
+    tv, fbp = t.tvopt(f, 2, 3, 4, 0.05, 1.0)
+    ref = [oracle.tvopt(f[s].astype(np.float64), prob["th"], prob["wpu"], 2, 3, 4, 0.05, 1.0, prec=64)[0]
+           for s in range(2)]
+    assert rel(tv, np.stack(ref), prob["mask"]) < TV_TOL
+
+
+def test_f64_solver_matches_fp64_oracle(prob):
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    a = prob["args"]
+    tv, fbp = t.tvopt(torch.from_numpy(prob["f"][:2].astype(np.float64)).cuda(), a["ninner"], a["nouter"],
+                      a["ncg"], a["lam"], a["mu"])
+    assert rel(tv, prob["tv64"][:2]) < 1e-9
+    assert rel(fbp, prob["fbp64"][:2]) < 1e-11
+
+
+def test_zero_slice_stays_finite(prob):
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    f = torch.zeros(2, prob["T"], prob["N"], device="cuda")
+    f[1] = torch.from_numpy(prob["f"][0]).cuda()
+    tv, fbp = t.tvopt(f, 1, 2, 3, 0.05, 1.0)
+    assert torch.isfinite(tv).all()
+    assert torch.count_nonzero(tv[0]) == 0
+
+
+def test_verbose_reports_err_diff(prob, capfd):
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    t.set_option(4, 1)
+    t.set_option(5, 2)
+    f = torch.from_numpy(prob["f"][:2]).cuda()
+    t.tvopt(f, 1, 4, 3, 0.05, 1.0)
+    out = capfd.readouterr().out
+    assert out.count("Slice:") == 4 and "delta:" in out
+    d = t.last_delta(2)
+    assert np.all(d > 0)
