@@ -40,6 +40,7 @@ P = ctypes.c_void_p
 I = ctypes.c_int
 F = ctypes.c_float
 D = ctypes.c_double
+L = ctypes.c_long
 
 # name -> argument types; every function returns int
 SIGNATURES = {
@@ -65,6 +66,20 @@ SIGNATURES = {
     "acu_tvopt_plain_dev": [P, I, P, I, I, I, F, F, P, P],
     "acu_tvopt_dev_f64": [P, I, P, I, I, I, D, D, P, P],
     "acu_tv_last_delta": [P, I, P],
+    "acu_tv_begin": [P, I, P, I, I, F, F, P],
+    "acu_tv_iterate": [P, I],
+    "acu_tv_end": [P, P],
+    "acu_frame_average_u16_dev": [P, I, L, P, P],
+    "acu_frame_average_dev": [P, I, L, P, P],
+    "acu_normalize_u16_dev": [P, I, I, L, P, P, P, P],
+    "acu_normalize_dev": [P, I, I, L, P, P, P, P],
+    "acu_pick_angle_dev": [P, I, P, L, P, F, P],
+    "acu_register_dev": [P, I, I, P, P, P, P, P],
+    "acu_xcorr_register_dev": [P, I, I, P, P, I, P, P, P],
+    "acu_median27_dev": [P, I, I, P, P, P, P],
+    "acu_resample_dev": [P, I, I, P, F, F, P],
+    "acu_proj_to_sino_dev": [P, I, I, I, P, F, F, P],
+    "acu_proj_to_sino_u16": [P, I, I, I, P, P, I, P, I, P, I, I, P, P, P],
 }
 
 

@@ -2,6 +2,7 @@
 // per-slice split-Bregman TV solvers (tomography/tv_hpc.F90:1-390).
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -9,92 +10,13 @@
 #include <string>
 #include <vector>
 
-#include "../../include/acumen_gpu.h"
-#include "kernels.h"
+#include "ctx.h"
 #include "tables.h"
 
 using namespace acu;
 
-namespace {
-
+namespace acu {
 thread_local std::string g_last_error;
-
-struct DevBuf {
-    void* p = nullptr;
-    size_t n = 0;
-    DevBuf() = default;
-    DevBuf(const DevBuf&) = delete;
-    DevBuf& operator=(const DevBuf&) = delete;
-    ~DevBuf() { release(); }
-    void release()
-    {
-        if (p) cudaFree(p);
-        p = nullptr;
-        n = 0;
-    }
-    // grow-only; returns a cudaError_t
-    cudaError_t ensure(size_t bytes)
-    {
-        if (bytes <= n && p) return cudaSuccess;
-        release();
-        if (bytes == 0) bytes = 16;
-        cudaError_t e = cudaMalloc(&p, bytes);
-        if (e != cudaSuccess) {
-            p = nullptr;
-            return e;
-        }
-        n = bytes;
-        return cudaSuccess;
-    }
-    template <typename T>
-    T* as() const { return reinterpret_cast<T*>(p); }
-};
-
-template <typename Real>
-struct GeomSet {
-    bool ready = false;
-    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_tw;
-    DevGeom<Real> d;
-};
-
-// Work buffers of the TV solver for one precision (lane layout, G groups).
-template <typename Real>
-struct TvState {
-    DevBuf f, fk, ruk, rp, q;                                   // T*N per slice
-    DevBuf uk, ukp, dx, dy, bx, by, rhs, r, p, Ap, tmp;         // N*N per slice
-    DevBuf rsold, alpha, beta, delta, part;                     // FP64 scalars
-    cudaGraphExec_t graph = nullptr;
-    std::string graph_key;
-    ~TvState()
-    {
-        if (graph) cudaGraphExecDestroy(graph);
-    }
-};
-
-}  // namespace
-
-struct acu_ctx {
-    int N = 0, T = 0, wpu = 0;
-    std::vector<float> theta;
-    cudaStream_t stream = nullptr;
-    cudaStream_t own_stream = nullptr;
-    int opt_filter = 0;  // FFT ramp filter
-    int opt_lanes = 0;
-    int opt_graph = 1;
-    int opt_verbose = 0;
-    int opt_print_every = 50;
-    int opt_slice_base = 1;
-    std::string err;
-    GeomSet<float> g32;
-    GeomSet<double> g64;
-    // operator work buffers
-    DevBuf w_in, w_out, w_q, w_host_in, w_host_out;
-    TvState<float> tv32;
-    TvState<double> tv64;
-    std::vector<double> last_delta;
-};
-
-namespace {
 
 int set_err(acu_ctx* ctx, int code, const char* fmt, ...)
 {
@@ -107,22 +29,9 @@ int set_err(acu_ctx* ctx, int code, const char* fmt, ...)
     g_last_error = buf;
     return code;
 }
+}  // namespace acu
 
-#define CK(ctx, call)                                                                           \
-    do {                                                                                        \
-        cudaError_t e_ = (call);                                                                \
-        if (e_ != cudaSuccess)                                                                  \
-            return set_err(ctx, e_ == cudaErrorMemoryAllocation ? ACU_ERR_NOMEM : ACU_ERR_CUDA, \
-                           "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
-    } while (0)
-
-#define CKLAUNCH(ctx) CK(ctx, cudaGetLastError())
-
-#define CKRET(expr)              \
-    do {                         \
-        int r_ = (expr);         \
-        if (r_ != ACU_OK) return r_; \
-    } while (0)
+namespace {
 
 template <typename Real>
 GeomSet<Real>& geomset(acu_ctx* c);
@@ -166,6 +75,19 @@ int ensure_geom(acu_ctx* c)
     gs.d.fft_h = gs.fft_h.template as<Real>();
     gs.d.fft_tw = gs.fft_tw.template as<float2>();
     gs.d.fft_tw64 = gs.fft_tw.template as<double2>();
+    {
+        // angle order of the pair projector: angles read through the x-pair
+        // image (|sin| >= |cos|) first, then the transposed ones
+        std::vector<int> ord;
+        for (int pass = 0; pass < 2; ++pass)
+            for (int t = 0; t < c->T; ++t) {
+                const bool tr = std::fabs((double)h.sc_fp[2 * t + 1]) > std::fabs((double)h.sc_fp[2 * t]);
+                if (tr == (pass == 1)) ord.push_back(t);
+            }
+        CK(c, gs.fp_order.ensure(sizeof(int) * ord.size()));
+        CK(c, cudaMemcpy(gs.fp_order.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
+        gs.d.fp_order = gs.fp_order.template as<int>();
+    }
     gs.d.fft_L = h.fft_L;
     gs.d.fft_log2L = h.fft_log2L;
     gs.ready = true;
@@ -233,7 +155,16 @@ int run_op_v(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
         CK(c, c->w_q.ensure(sizeof(Real) * nsino * G * V));
         lanes_iradon<Real, V>(c, g, G, lin, c->w_q.template as<Real>(), lout);
         break;
-    case OP_RADON: launch_radon<Real, V>(g, G, lin, lout, c->stream); break;
+    case OP_RADON:
+        if constexpr (V == 4 && sizeof(Real) == 4) {
+            CK(c, c->pairP.ensure(sizeof(float) * 8 * nimg * G));
+            CK(c, c->pairPT.ensure(sizeof(float) * 8 * nimg * G));
+            launch_radon_pairs(g, G, lin, c->pairP.template as<float>(), c->pairPT.template as<float>(), lout,
+                               c->stream);
+        } else {
+            launch_radon<Real, V>(g, G, lin, lout, c->stream);
+        }
+        break;
     case OP_RADON_ADJ: launch_radon_adjoint<Real, V>(g, G, lin, lout, c->stream); break;
     case OP_FILTER: lanes_filter<Real, V>(c, g, G, lin, lout); break;
     case OP_BACKPROJECT: launch_backproject<Real, V>(g, G, lin, lout, c->stream); break;
@@ -298,7 +229,14 @@ struct TvRun {
     Real* B(DevBuf& b) const { return b.template as<Real>(); }
 
     void iradon(const Real* sino, Real* img) { lanes_iradon<Real, V>(c, *g, G, sino, B(s->q), img); }
-    void radon(const Real* img, Real* sino) { launch_radon<Real, V>(*g, G, img, sino, c->stream); }
+    void radon(const Real* img, Real* sino)
+    {
+        if constexpr (V == 4 && sizeof(Real) == 4)
+            launch_radon_pairs(*g, G, img, c->pairP.template as<float>(), c->pairPT.template as<float>(), sino,
+                               c->stream);
+        else
+            launch_radon<Real, V>(*g, G, img, sino, c->stream);
+    }
 
     // One Bregman outer iteration (tv_hpc.F90:206-346).  On entry ruk holds
     // radon(uk) for the current uk, which the first inner iteration reuses.
@@ -333,8 +271,25 @@ struct TvRun {
 };
 
 template <typename Real, int V>
-int tv_solve_v(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int ncg, Real lambda, Real mu,
-               Real* d_tv, Real* d_fbp)
+TvRun<Real, V> make_run(acu_ctx* c, TvState<Real>& s)
+{
+    TvRun<Real, V> run;
+    run.c = c;
+    run.g = &geomset<Real>(c).d;
+    run.s = &s;
+    run.N = c->N; run.T = c->T; run.G = s.G; run.S = s.S;
+    run.ninner = s.ninner; run.ncg = s.ncg; run.lambda = (Real)s.lambda; run.mu = (Real)s.mu;
+    run.verbose = c->opt_verbose != 0;
+    run.sc = TvScalars{s.rsold.template as<double>(), s.alpha.template as<double>(), s.beta.template as<double>(),
+                       s.delta.template as<double>(), s.part.template as<double>(), s.nblk};
+    return run;
+}
+
+// Allocates the solver state for S slices, copies f in, and runs the warm
+// start and initialisation of tv_hpc.F90:172-202 (FBP, d = b = 0, fk = f),
+// plus radon(uk) for the first inner iteration.
+template <typename Real, int V>
+int tv_begin_v(acu_ctx* c, int S, const Real* d_f, int ninner, int ncg, double lambda, double mu, Real* d_fbp)
 {
     CKRET(ensure_geom<Real>(c));
     TvState<Real>& s = tvstate<Real>(c);
@@ -344,23 +299,19 @@ int tv_solve_v(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int n
     for (DevBuf* b : {&s.uk, &s.dx, &s.dy, &s.bx, &s.by, &s.rhs, &s.r, &s.p, &s.Ap, &s.tmp})
         CK(c, b->ensure(sizeof(Real) * nimg));
     if (c->opt_verbose) CK(c, s.ukp.ensure(sizeof(Real) * nimg));
+    if constexpr (V == 4 && sizeof(Real) == 4) {
+        CK(c, c->pairP.ensure(sizeof(float) * 2 * nimg));
+        CK(c, c->pairPT.ensure(sizeof(float) * 2 * nimg));
+    }
     const int Sp = G * V;
-    const int nblk = (int)std::min<size_t>(((size_t)N * N + 255) / 256, 512);
+    s.nblk = (int)std::min<size_t>(((size_t)N * N + 255) / 256, 512);
     for (DevBuf* b : {&s.rsold, &s.alpha, &s.beta, &s.delta}) CK(c, b->ensure(sizeof(double) * Sp));
-    CK(c, s.part.ensure(sizeof(double) * (size_t)nblk * Sp));
-
-    TvRun<Real, V> run;
-    run.c = c;
-    run.g = &geomset<Real>(c).d;
-    run.s = &s;
-    run.N = N; run.T = T; run.G = G; run.S = S;
-    run.ninner = ninner; run.ncg = ncg; run.lambda = lambda; run.mu = mu;
-    run.verbose = c->opt_verbose != 0;
-    run.sc = TvScalars{s.rsold.template as<double>(), s.alpha.template as<double>(), s.beta.template as<double>(), s.delta.template as<double>(),
-                       s.part.template as<double>(), nblk};
+    CK(c, s.part.ensure(sizeof(double) * (size_t)s.nblk * Sp));
+    s.S = S; s.G = G; s.V = V; s.ninner = ninner; s.ncg = ncg; s.lambda = lambda; s.mu = mu;
+    s.outer_done = 0;
+    s.active = true;
+    TvRun<Real, V> run = make_run<Real, V>(c, s);
     cudaStream_t st = c->stream;
-
-    // warm start and state initialisation (tv_hpc.F90:172-202)
     if constexpr (V > 1)
         launch_to_lanes<Real, V>(d_f, s.f.template as<Real>(), S, (size_t)T * N, st);
     else
@@ -376,12 +327,22 @@ int tv_solve_v(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int n
     CK(c, cudaMemcpyAsync(s.fk.p, s.f.p, sizeof(Real) * nsino, cudaMemcpyDeviceToDevice, st));
     run.radon(s.uk.template as<Real>(), s.ruk.template as<Real>());
     CKLAUNCH(c);
+    return ACU_OK;
+}
 
-    const bool use_graph = c->opt_graph != 0 && !run.verbose && nouter > 1;
+// nouter Bregman outer iterations (tv_hpc.F90:205-353) of the active problem.
+template <typename Real, int V>
+int tv_iterate_v(acu_ctx* c, int nouter)
+{
+    TvState<Real>& s = tvstate<Real>(c);
+    TvRun<Real, V> run = make_run<Real, V>(c, s);
+    cudaStream_t st = c->stream;
+    const int S = s.S, Sp = s.G * V;
+    const bool use_graph = c->opt_graph != 0 && !run.verbose;
     if (use_graph) {
         char key[256];
-        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.9g/%.9g/%d/%p/%p", (int)sizeof(Real), V, G, ninner, ncg,
-                 (double)lambda, (double)mu, c->opt_filter, s.uk.p, (void*)st);
+        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
+                 s.ncg, s.lambda, s.mu, c->opt_filter, s.uk.p, s.part.p);
         if (!s.graph || s.graph_key != key) {
             if (s.graph) {
                 cudaGraphExecDestroy(s.graph);
@@ -405,29 +366,81 @@ int tv_solve_v(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int n
             s.graph_key = key;
         }
         for (int jo = 0; jo < nouter; ++jo) CK(c, cudaGraphLaunch(s.graph, st));
-    } else {
-        c->last_delta.assign(S, 0.0);
-        for (int jo = 1; jo <= nouter; ++jo) {
-            run.outer_body();
-            CKLAUNCH(c);
-            if (run.verbose && (jo % c->opt_print_every == 0 || jo == nouter)) {
-                std::vector<double> dl(Sp);
-                CK(c, cudaMemcpyAsync(dl.data(), s.delta.p, sizeof(double) * Sp, cudaMemcpyDeviceToHost, st));
-                CK(c, cudaStreamSynchronize(st));
-                for (int k = 0; k < S; ++k) c->last_delta[k] = dl[k];
-                if (jo % c->opt_print_every == 0)
-                    for (int k = 0; k < S; ++k)
-                        printf(" Slice: %12d Loop: %12d delta: %15.8E\n", c->opt_slice_base + k, jo, dl[k]);
+        s.outer_done += nouter;
+        return ACU_OK;
+    }
+    if ((int)c->last_delta.size() != S) c->last_delta.assign(S, 0.0);
+    for (int k = 1; k <= nouter; ++k) {
+        run.outer_body();
+        CKLAUNCH(c);
+        const int jo = ++s.outer_done;
+        if (run.verbose && (jo % c->opt_print_every == 0 || k == nouter)) {
+            std::vector<double> dl(Sp);
+            CK(c, cudaMemcpyAsync(dl.data(), s.delta.p, sizeof(double) * Sp, cudaMemcpyDeviceToHost, st));
+            CK(c, cudaStreamSynchronize(st));
+            for (int i = 0; i < S; ++i) c->last_delta[i] = dl[i];
+            if (jo % c->opt_print_every == 0) {
+                for (int i = 0; i < S; ++i)
+                    printf(" Slice: %12d Loop: %12d delta: %15.8E\n", c->opt_slice_base + i, jo, dl[i]);
                 fflush(stdout);
             }
         }
     }
+    return ACU_OK;
+}
+
+template <typename Real, int V>
+int tv_end_v(acu_ctx* c, Real* d_tv)
+{
+    TvState<Real>& s = tvstate<Real>(c);
+    const size_t nimg = (size_t)c->N * c->N * s.G * V;
     if constexpr (V > 1)
-        launch_from_lanes<Real, V>(s.uk.template as<Real>(), d_tv, S, (size_t)N * N, st);
+        launch_from_lanes<Real, V>(s.uk.template as<Real>(), d_tv, s.S, (size_t)c->N * c->N, c->stream);
     else
-        CK(c, cudaMemcpyAsync(d_tv, s.uk.p, sizeof(Real) * nimg, cudaMemcpyDeviceToDevice, st));
+        CK(c, cudaMemcpyAsync(d_tv, s.uk.p, sizeof(Real) * nimg, cudaMemcpyDeviceToDevice, c->stream));
     CKLAUNCH(c);
     return ACU_OK;
+}
+
+template <typename Real>
+int tv_begin(acu_ctx* c, int S, const Real* d_f, int ninner, int ncg, double lambda, double mu, Real* d_fbp)
+{
+    CKRET(check_ctx(c, S));
+    if (S < 1) return set_err(c, ACU_ERR_INVALID, "nslices must be >= 1");
+    if (!d_f) return set_err(c, ACU_ERR_INVALID, "null array");
+    if (ninner < 0 || ncg < 0) return set_err(c, ACU_ERR_INVALID, "iteration counts must be >= 0");
+    if (lambda == 0.0) return set_err(c, ACU_ERR_INVALID, "lambda must be non-zero (shrink threshold 1/lambda)");
+    if constexpr (sizeof(Real) == 4) {
+        if (pick_lanes(c, S, false) == 4) return tv_begin_v<Real, 4>(c, S, d_f, ninner, ncg, lambda, mu, d_fbp);
+    }
+    return tv_begin_v<Real, 1>(c, S, d_f, ninner, ncg, lambda, mu, d_fbp);
+}
+
+template <typename Real>
+int tv_iterate(acu_ctx* c, int nouter)
+{
+    if (!c) return set_err(nullptr, ACU_ERR_INVALID, "null context");
+    TvState<Real>& s = tvstate<Real>(c);
+    if (!s.active) return set_err(c, ACU_ERR_INVALID, "no active TV problem: call acu_tv_begin first");
+    if (nouter < 0) return set_err(c, ACU_ERR_INVALID, "nouter must be >= 0");
+    if (nouter == 0) return ACU_OK;
+    if (s.V == 4) {
+        if constexpr (sizeof(Real) == 4) return tv_iterate_v<Real, 4>(c, nouter);
+    }
+    return tv_iterate_v<Real, 1>(c, nouter);
+}
+
+template <typename Real>
+int tv_end(acu_ctx* c, Real* d_tv)
+{
+    if (!c) return set_err(nullptr, ACU_ERR_INVALID, "null context");
+    TvState<Real>& s = tvstate<Real>(c);
+    if (!s.active) return set_err(c, ACU_ERR_INVALID, "no active TV problem: call acu_tv_begin first");
+    if (!d_tv) return set_err(c, ACU_ERR_INVALID, "null array");
+    if (s.V == 4) {
+        if constexpr (sizeof(Real) == 4) return tv_end_v<Real, 4>(c, d_tv);
+    }
+    return tv_end_v<Real, 1>(c, d_tv);
 }
 
 template <typename Real>
@@ -437,14 +450,10 @@ int tv_solve(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int ncg
     CKRET(check_ctx(c, S));
     if (S == 0) return ACU_OK;
     if (!d_f || !d_tv) return set_err(c, ACU_ERR_INVALID, "null array");
-    if (ninner < 0 || nouter < 0 || ncg < 0)
-        return set_err(c, ACU_ERR_INVALID, "iteration counts must be >= 0");
-    if (lambda == Real(0)) return set_err(c, ACU_ERR_INVALID, "lambda must be non-zero (shrink threshold 1/lambda)");
-    if constexpr (sizeof(Real) == 4) {
-        if (pick_lanes(c, S, false) == 4)
-            return tv_solve_v<Real, 4>(c, S, d_f, ninner, nouter, ncg, lambda, mu, d_tv, d_fbp);
-    }
-    return tv_solve_v<Real, 1>(c, S, d_f, ninner, nouter, ncg, lambda, mu, d_tv, d_fbp);
+    if (nouter < 0) return set_err(c, ACU_ERR_INVALID, "iteration counts must be >= 0");
+    CKRET(tv_begin<Real>(c, S, d_f, ninner, ncg, (double)lambda, (double)mu, d_fbp));
+    CKRET(tv_iterate<Real>(c, nouter));
+    return tv_end<Real>(c, d_tv);
 }
 
 // ---- per-slice comparator: the reference's loop structure on the GPU ---------
@@ -696,6 +705,13 @@ int acu_tvopt_dev_f64(acu_ctx* c, int S, const double* f, int ninner, int nouter
 {
     return tv_solve<double>(c, S, f, ninner, nouter, ncg, lambda, mu, tv, fbp);
 }
+
+int acu_tv_begin(acu_ctx* c, int S, const float* d_f, int ninner, int ncg, float lambda, float mu, float* d_fbp)
+{
+    return tv_begin<float>(c, S, d_f, ninner, ncg, lambda, mu, d_fbp);
+}
+int acu_tv_iterate(acu_ctx* c, int nouter) { return tv_iterate<float>(c, nouter); }
+int acu_tv_end(acu_ctx* c, float* d_tv) { return tv_end<float>(c, d_tv); }
 
 int acu_tv_last_delta(const acu_ctx* c, int S, double* delta)
 {

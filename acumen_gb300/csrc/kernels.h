@@ -21,6 +21,7 @@ struct DevGeom {
     const float2* fft_tw = nullptr; // [L/2] twiddles exp(-2 pi i k / L) (float)
     const double2* fft_tw64 = nullptr;
     int fft_L = 0, fft_log2L = 0;
+    const int* fp_order = nullptr;  // [T] projector angles, |sin| >= |cos| first
 };
 
 // ---- radon operators (kernels_radon.cu); arrays in lane layout ------------
@@ -28,6 +29,10 @@ template <typename Real, int V>
 void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st);
 template <typename Real, int V>
 void launch_radon(const DevGeom<Real>& g, int G, const Real* img, Real* sino, cudaStream_t st);
+// Projector through pair images (float, 4 slices per thread): P and PT are
+// work buffers of 2 * N * N * 4 floats per slice group each.
+void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float* P, float* PT, float* sino,
+                        cudaStream_t st);
 template <typename Real, int V>
 void launch_radon_adjoint(const DevGeom<Real>& g, int G, const Real* sino, Real* img, cudaStream_t st);
 template <typename Real, int V>

@@ -1,0 +1,340 @@
+// Projection preprocessing kernels: flat/dark averages and log-normalisation
+// (tomography/fits_to_hpc.F90:183-244), the 0/180-degree pick
+// (projections_to_sinogram_hpc.F90:141-224), rotation-axis registration
+// (:231-364, plus a cross-correlation variant), the 27-point median (:426-452),
+// the bilinear resample (:456-470) and the transpose to slice-major sinograms
+// (:481-487).
+//
+// Arithmetic that decides an index or a comparison is written with explicit
+// round-to-nearest operations so that it matches the single-precision
+// reference operation for operation.
+#include "common.cuh"
+#include "prep.h"
+
+namespace acu {
+
+template <typename Tin>
+__device__ __forceinline__ float to_f(Tin v) { return (float)v; }
+
+// ---- frame averages (fits_to_hpc.F90:183-210): running sum in frame order ----
+template <typename Tin>
+__global__ void k_frame_average(int nframes, long npix, const Tin* __restrict__ frames, float* __restrict__ out)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < npix; i += (long)gridDim.x * blockDim.x) {
+        float s = 0.0f;
+        for (int j = 0; j < nframes; ++j) s = __fadd_rn(s, to_f(frames[(size_t)j * npix + i]));
+        out[i] = __fdiv_rn(s, (float)nframes);
+    }
+}
+
+// ---- log-normalisation (fits_to_hpc.F90:243 mode 0, :244 mode 1) ------------
+template <typename Tin>
+__global__ void k_normalize(int mode, long npix, long total, const Tin* __restrict__ raw, const float* __restrict__ ob,
+                            const float* __restrict__ df, float* __restrict__ out)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const long k = i % npix;
+        const float I = to_f(raw[i]);
+        float v;
+        if (mode == 0) {
+            v = -logf(__fdiv_rn(I, fmaxf(ob[k], 1.0f)));
+        } else {
+            const float d = df[k];
+            v = -logf(__fdiv_rn(fmaxf(__fsub_rn(I, d), 1e-16f), fmaxf(__fsub_rn(ob[k], d), 1.0f)));
+        }
+        out[i] = v;
+    }
+}
+
+// ---- lerp between two projections (projections_to_sinogram_hpc.F90:162) ------
+__global__ void k_lerp(long n, const float* __restrict__ a, const float* __restrict__ b, float ta, float tb,
+                       float target, float* __restrict__ out)
+{
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        out[i] = __fadd_rn(__fdiv_rn(__fmul_rn(__fsub_rn(target, ta), __fsub_rn(b[i], a[i])), __fsub_rn(tb, ta)),
+                           a[i]);
+}
+
+// ---- bilinear resample with the reference's clamps (:456-470) ---------------
+struct ResampleGeom {
+    int ndet, nrows, add;
+    float cth, sth, shift;
+};
+
+__device__ __forceinline__ float resample_at(const ResampleGeom& g, const float* __restrict__ src, int jx, int jy)
+{
+    const float mx = __fdiv_rn((float)(g.ndet + g.add - 1), 2.0f);
+    const float my = __fdiv_rn((float)(g.nrows - 1), 2.0f);
+    const float ss = (float)g.ndet;
+    const float ax = __fsub_rn(__fsub_rn((float)jx, mx), __fmul_rn(ss, g.shift));
+    const float ay = __fsub_rn((float)jy, my);
+    float xr = __fadd_rn(__fsub_rn(__fmul_rn(g.cth, ax), __fmul_rn(g.sth, ay)), mx);
+    float yr = __fadd_rn(__fadd_rn(__fmul_rn(g.sth, ax), __fmul_rn(g.cth, ay)), my);
+    xr = fminf(fmaxf(xr, 1.0f), (float)g.ndet);
+    yr = fminf(fmaxf(yr, 1.0f), (float)g.nrows);
+    int y1 = min(max((int)floorf(yr), 1), g.nrows);
+    int y2 = min(max(y1 + 1, 1), g.nrows);
+    int x1 = min(max((int)floorf(xr), 1), g.ndet);
+    int x2 = min(max(x1 + 1, 1), g.ndet);
+    const float wxl = __fsub_rn((float)x2, xr), wxh = __fsub_rn(xr, (float)x1);
+    const float wyl = __fsub_rn((float)y2, yr), wyh = __fsub_rn(yr, (float)y1);
+    const size_t r1 = (size_t)(y1 - 1) * g.ndet, r2 = (size_t)(y2 - 1) * g.ndet;
+    float acc = __fmul_rn(__fmul_rn(src[r1 + x1 - 1], wxl), wyl);
+    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(src[r1 + x2 - 1], wxh), wyl));
+    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(src[r2 + x1 - 1], wxl), wyh));
+    acc = __fadd_rn(acc, __fmul_rn(__fmul_rn(src[r2 + x2 - 1], wxh), wyh));
+    return acc;
+}
+
+__global__ void k_resample(ResampleGeom g, const float* __restrict__ src, float* __restrict__ out)
+{
+    const int nx = g.ndet + g.add;
+    const long n = (long)nx * g.nrows;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int jx = (int)(i % nx) + 1, jy = (int)(i / nx) + 1;
+        out[i] = resample_at(g, src, jx, jy);
+    }
+}
+
+// ---- registration objective (:279-284 / :308-313 / :346-351) ----------------
+// sum |V0(jx,jy) - V180(nx-jx+1,jy)| over the padded grid: one FP64 partial
+// per block, summed afterwards in block order (deterministic).
+__global__ void __launch_bounds__(256) k_mirror_error(ResampleGeom g, const float* __restrict__ p0,
+                                                      const float* __restrict__ p180, double* __restrict__ part)
+{
+    __shared__ double sh[32];
+    const int nx = g.ndet + g.add;
+    const long n = (long)nx * g.nrows;
+    double acc = 0.0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int jx = (int)(i % nx) + 1, jy = (int)(i / nx) + 1;
+        const float a = resample_at(g, p0, jx, jy);
+        const float b = resample_at(g, p180, nx - jx + 1, jy);
+        acc += (double)fabsf(__fsub_rn(a, b));
+    }
+    const double r = block_sum(acc, sh);
+    if (threadIdx.x == 0 && threadIdx.y == 0) part[blockIdx.x] = r;
+}
+
+// centre-of-mass sums (:234-243): tm, cmx_0, cmx_180 as FP64 partials
+__global__ void __launch_bounds__(256) k_com(int ndet, int nrows, int add, const float* __restrict__ p0,
+                                             const float* __restrict__ p180, double* __restrict__ part)
+{
+    __shared__ double sh[32];
+    double tm = 0.0, c0 = 0.0, c1 = 0.0;
+    const long n = (long)ndet * nrows;
+    const float nda = (float)(ndet + add);
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int jx = (int)(i % ndet) + 1;
+        const float a = p0[i], b = p180[i];
+        const float w = __fsub_rn(__fsub_rn(__fdiv_rn(__fmul_rn(__fmul_rn(2.0f, nda), (float)(jx - 1)),
+                                                      (float)(ndet + add - 1)),
+                                            (float)ndet),
+                                  (float)add);
+        tm += (double)a + (double)b;
+        c0 += (double)__fmul_rn(a, w);
+        c1 += (double)__fmul_rn(b, w);
+    }
+    double r = block_sum(tm, sh);
+    if (threadIdx.x == 0) part[3 * blockIdx.x] = r;
+    r = block_sum(c0, sh);
+    if (threadIdx.x == 0) part[3 * blockIdx.x + 1] = r;
+    r = block_sum(c1, sh);
+    if (threadIdx.x == 0) part[3 * blockIdx.x + 2] = r;
+}
+
+// fixed-order sum of `n` partials with stride `stride` (offset `off`) into out[0]
+__global__ void k_sum_partials(const double* __restrict__ part, int n, int stride, int off, double* __restrict__ out)
+{
+    __shared__ double sh[32];
+    double v = 0.0;
+    for (int i = threadIdx.x; i < n; i += blockDim.x) v += part[(size_t)i * stride + off];
+    const double r = block_sum(v, sh);
+    if (threadIdx.x == 0) out[0] = r;
+}
+
+// ---- cross-correlation registration (new) --------------------------------------
+// C(k) = sum_{x,y} p0(x,y) * p180(ndet-1-x+k, y) with every product truncated
+// to 2^-32 fixed point: integer sums do not depend on their order, so the
+// argmax is bit-exact against the CPU oracle.
+__device__ __forceinline__ long long fx_prod(float a, float b)
+{
+    const double p = (double)a * (double)b;
+    return __double2ll_rd(p * 4294967296.0);
+}
+
+__global__ void __launch_bounds__(256) k_xcorr(int ndet, int nrows, int kmax, const float* __restrict__ p0,
+                                               const float* __restrict__ p180, unsigned long long* __restrict__ corr)
+{
+    const int k = (int)blockIdx.y - kmax;
+    const long n = (long)ndet * nrows;
+    long long acc = 0;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
+        const int x = (int)(i % ndet), y = (int)(i / ndet);
+        const int xm = ndet - 1 - x + k;
+        if (xm >= 0 && xm < ndet) acc += fx_prod(p0[i], p180[(size_t)y * ndet + xm]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(&corr[blockIdx.y], (unsigned long long)acc);
+}
+
+// Warp-shuffle argmax over the nk correlation values (ties: lowest index).
+__global__ void k_argmax(int nk, const unsigned long long* __restrict__ corr, int* __restrict__ best)
+{
+    long long bv = LLONG_MIN;
+    int bi = 0x7fffffff;
+    for (int i = threadIdx.x; i < nk; i += 32) {
+        const long long v = (long long)corr[i];
+        if (v > bv || (v == bv && i < bi)) { bv = v; bi = i; }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const long long ov = __shfl_down_sync(0xffffffffu, bv, o);
+        const int oi = __shfl_down_sync(0xffffffffu, bi, o);
+        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+    }
+    if (threadIdx.x == 0) best[0] = bi;
+}
+
+// ---- 27-point median (:426-452): the reference's descending exchange sort,
+// passes 1..14 (the later passes do not touch element 14), with the
+// intended slots 1..27 ------------------------------------------------------------
+__global__ void __launch_bounds__(128) k_median27(int ndet, int nrows, int nproj_chunk, int p_first, int nfiles,
+                                                  const float* __restrict__ proj, float* __restrict__ out)
+{
+    const long npix = (long)ndet * nrows;
+    const long total = npix * nproj_chunk;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int pc = (int)(i / npix);
+        const long k = i % npix;
+        const int p = p_first + pc;
+        const int jx = (int)(k % ndet) + 1, jy = (int)(k / ndet) + 1;
+        const float* dc = proj + (size_t)p * npix;
+        const float* dl = p > 0 ? dc - npix : dc;
+        const float* dr = p < nfiles - 1 ? dc + npix : dc;
+        float r[27];
+#pragma unroll
+        for (int jxs = -1; jxs <= 1; ++jxs)
+#pragma unroll
+            for (int jys = -1; jys <= 1; ++jys) {
+                const int cx = min(max(jx + jxs, 1), ndet), cy = min(max(jy + jys, 1), nrows);
+                const size_t o = (size_t)(cy - 1) * ndet + (cx - 1);
+                const int slot = 3 * (jxs + 1) + (jys + 1);
+                r[slot] = __ldg(dl + o);
+                r[slot + 9] = __ldg(dc + o);
+                r[slot + 18] = __ldg(dr + o);
+            }
+#pragma unroll
+        for (int a = 0; a < 14; ++a) {
+            float ra = r[a];
+#pragma unroll
+            for (int b = a + 1; b < 27; ++b) {
+                const float rb = r[b];
+                const bool sw = rb > ra;
+                r[b] = sw ? ra : rb;
+                ra = sw ? rb : ra;
+            }
+            r[a] = ra;
+        }
+        out[(size_t)pc * npix + k] = r[13];
+    }
+}
+
+// resample + transpose of a chunk of projections into the slice-major
+// sinograms sino[row][projection][det] (:456-487)
+__global__ void k_resample_to_sino(ResampleGeom g, int nproj_chunk, int p_first, int nfiles,
+                                   const float* __restrict__ med, float* __restrict__ sino)
+{
+    const int nx = g.ndet + g.add;
+    const long per = (long)nx * g.nrows;
+    const long total = per * nproj_chunk;
+    const long npix = (long)g.ndet * g.nrows;
+    for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < total; i += (long)gridDim.x * blockDim.x) {
+        const int pc = (int)(i / per);
+        const long k = i % per;
+        const int jx = (int)(k % nx) + 1, jy = (int)(k / nx) + 1;
+        const float v = resample_at(g, med + (size_t)pc * npix, jx, jy);
+        sino[((size_t)(jy - 1) * nfiles + (p_first + pc)) * nx + (jx - 1)] = v;
+    }
+}
+
+// ---- launchers -----------------------------------------------------------------
+static inline unsigned nblocks(long n, int threads, unsigned cap = 8192)
+{
+    long b = (n + threads - 1) / threads;
+    return (unsigned)(b < (long)cap ? (b < 1 ? 1 : b) : cap);
+}
+
+void launch_frame_average_u16(int nf, long npix, const uint16_t* f, float* out, cudaStream_t st)
+{
+    k_frame_average<uint16_t><<<nblocks(npix, 256), 256, 0, st>>>(nf, npix, f, out);
+}
+void launch_frame_average_f32(int nf, long npix, const float* f, float* out, cudaStream_t st)
+{
+    k_frame_average<float><<<nblocks(npix, 256), 256, 0, st>>>(nf, npix, f, out);
+}
+void launch_normalize_u16(int mode, int nproj, long npix, const uint16_t* raw, const float* ob, const float* df,
+                          float* out, cudaStream_t st)
+{
+    const long total = npix * nproj;
+    k_normalize<uint16_t><<<nblocks(total, 256), 256, 0, st>>>(mode, npix, total, raw, ob, df, out);
+}
+void launch_normalize_f32(int mode, int nproj, long npix, const float* raw, const float* ob, const float* df,
+                          float* out, cudaStream_t st)
+{
+    const long total = npix * nproj;
+    k_normalize<float><<<nblocks(total, 256), 256, 0, st>>>(mode, npix, total, raw, ob, df, out);
+}
+void launch_lerp(long n, const float* a, const float* b, float ta, float tb, float target, float* out,
+                 cudaStream_t st)
+{
+    k_lerp<<<nblocks(n, 256), 256, 0, st>>>(n, a, b, ta, tb, target, out);
+}
+void launch_resample(int ndet, int nrows, const float* src, float cth, float sth, float shift, float* out,
+                     cudaStream_t st)
+{
+    ResampleGeom g{ndet, nrows, ndet % 2 == 0 ? 1 : 0, cth, sth, shift};
+    k_resample<<<nblocks((long)(ndet + g.add) * nrows, 256), 256, 0, st>>>(g, src, out);
+}
+int mirror_error_blocks(int ndet, int nrows)
+{
+    return (int)nblocks((long)(ndet + 1) * nrows, 256, 1024);
+}
+void launch_mirror_error(int ndet, int nrows, const float* p0, const float* p180, float cth, float sth, float shift,
+                         double* part, int nblk, double* out, cudaStream_t st)
+{
+    ResampleGeom g{ndet, nrows, ndet % 2 == 0 ? 1 : 0, cth, sth, shift};
+    k_mirror_error<<<nblk, 256, 0, st>>>(g, p0, p180, part);
+    k_sum_partials<<<1, 256, 0, st>>>(part, nblk, 1, 0, out);
+}
+void launch_com(int ndet, int nrows, const float* p0, const float* p180, double* part, int nblk, double* out3,
+                cudaStream_t st)
+{
+    k_com<<<nblk, 256, 0, st>>>(ndet, nrows, ndet % 2 == 0 ? 1 : 0, p0, p180, part);
+    for (int j = 0; j < 3; ++j) k_sum_partials<<<1, 256, 0, st>>>(part, nblk, 3, j, out3 + j);
+}
+void launch_xcorr(int ndet, int nrows, int kmax, const float* p0, const float* p180, unsigned long long* corr,
+                  int* best, cudaStream_t st)
+{
+    const int nk = 2 * kmax + 1;
+    cudaMemsetAsync(corr, 0, sizeof(unsigned long long) * nk, st);
+    dim3 grd(nblocks((long)ndet * nrows, 256, 64), nk);
+    k_xcorr<<<grd, 256, 0, st>>>(ndet, nrows, kmax, p0, p180, corr);
+    k_argmax<<<1, 32, 0, st>>>(nk, corr, best);
+}
+void launch_median27(int ndet, int nrows, int nchunk, int p_first, int nfiles, const float* proj, float* out,
+                     cudaStream_t st)
+{
+    k_median27<<<nblocks((long)ndet * nrows * nchunk, 128, 65535), 128, 0, st>>>(ndet, nrows, nchunk, p_first,
+                                                                                nfiles, proj, out);
+}
+void launch_resample_to_sino(int ndet, int nrows, int nchunk, int p_first, int nfiles, const float* med,
+                             float cth, float sth, float shift, float* sino, cudaStream_t st)
+{
+    ResampleGeom g{ndet, nrows, ndet % 2 == 0 ? 1 : 0, cth, sth, shift};
+    k_resample_to_sino<<<nblocks((long)(ndet + g.add) * nrows * nchunk, 256, 65535), 256, 0, st>>>(
+        g, nchunk, p_first, nfiles, med, sino);
+}
+
+}  // namespace acu

@@ -123,6 +123,137 @@ void launch_radon(const DevGeom<Real>& g, int G, const Real* img, Real* sino, cu
 }
 
 // ---------------------------------------------------------------------------
+// Projector over "pair" images (single precision, 4 slices per thread).
+//
+// The bilinear sample needs (x1,y1), (x1+1,y1), (x1,y1+1), (x1+1,y1+1).  A
+// gather of four separate 16-byte taps per lane makes the L1 data pipe the
+// limit (one wavefront per distinct sector).  Here the image is re-laid as
+// pairs: P[g][y][x] = (pixel(x,y), pixel(x+1,y)) for the 4 slices, 32 bytes,
+// and the transposed PT[g][x][y] = (pixel(x,y), pixel(x,y+1)).  One 256-bit
+// load then fetches two taps, and for every angle the kernel reads the copy
+// in which the warp's 32 adjacent rays (offset (-sin, cos) per lane) spread
+// along the pair axis, so consecutive lanes hit consecutive sectors.
+// The arithmetic is identical to k_radon.
+// ---------------------------------------------------------------------------
+struct __align__(32) Pair4 {
+    float a[4];   // first pixel, 4 slices
+    float b[4];   // second pixel
+};
+
+__device__ __forceinline__ Pair4 ld_pair(const float* p)
+{
+    Pair4 r;
+    asm("ld.global.nc.v8.f32 {%0,%1,%2,%3,%4,%5,%6,%7}, [%8];"
+        : "=f"(r.a[0]), "=f"(r.a[1]), "=f"(r.a[2]), "=f"(r.a[3]), "=f"(r.b[0]), "=f"(r.b[1]), "=f"(r.b[2]),
+          "=f"(r.b[3])
+        : "l"(p));
+    return r;
+}
+
+// Builds P and PT from a lane-layout image (V = 4).  32x32 pixel tiles; the
+// transposed copy goes through shared memory so both stores are coalesced.
+__global__ void __launch_bounds__(256) k_make_pairs(const float* __restrict__ img, float* __restrict__ P,
+                                                    float* __restrict__ PT, int N)
+{
+    __shared__ float4 tile[33][33];
+    const int g = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const float4* src = reinterpret_cast<const float4*>(img) + (size_t)g * N * N;
+    for (int i = threadIdx.x; i < 33 * 33; i += blockDim.x) {
+        const int ty = i / 33, tx = i % 33;
+        const int x = x0 + tx, y = y0 + ty;
+        tile[ty][tx] = (x < N && y < N) ? src[(size_t)y * N + x] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    float4* Pg = reinterpret_cast<float4*>(P) + (size_t)g * N * N * 2;
+    float4* PTg = reinterpret_cast<float4*>(PT) + (size_t)g * N * N * 2;
+    for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+        const int ty = i / 32, tx = i % 32;
+        const int x = x0 + tx, y = y0 + ty;
+        if (x < N && y < N) {
+            const size_t o = ((size_t)y * N + x) * 2;
+            Pg[o] = tile[ty][tx];
+            Pg[o + 1] = tile[ty][tx + 1];
+        }
+        // transposed: row = x, column = y; consecutive threads walk y
+        const int xt = x0 + ty, yt = y0 + tx;
+        if (xt < N && yt < N) {
+            const size_t o = ((size_t)xt * N + yt) * 2;
+            PTg[o] = tile[tx][ty];
+            PTg[o + 1] = tile[tx + 1][ty];
+        }
+    }
+}
+
+// Each warp covers 8 adjacent rays x 4 interleaved step phases of one angle:
+// lane = ray (lane % 8) and phase (lane / 8); a lane sums the samples
+// jx = 1 + phase + 4k of its ray, and the four phase sums of a ray are added
+// with two butterfly shuffles ((p0 + p1) + (p2 + p3) in a fixed order).  The
+// 32 samples of one load instruction then form a compact 8 x 4 patch, which
+// touches fewer cache lines than 32 rays side by side.  Blocks take angles in
+// the order `order` (angles read through P first, then those read through
+// PT), so one pair image at a time is live in L2.
+__global__ void __launch_bounds__(128) k_radon_pairs(const float* __restrict__ P, const float* __restrict__ PT,
+                                                     const float* __restrict__ sc, const int* __restrict__ order,
+                                                     float* __restrict__ sino, int N, int T, float mid)
+{
+    const int lane = threadIdx.x & 31;
+    const int ray = lane & 7, phase = lane >> 3;
+    const int jy = blockIdx.x * 32 + threadIdx.y * 8 + ray + 1;
+    const int t = order[blockIdx.y];
+    const int g = blockIdx.z;
+    const float s = sc[2 * t], c = sc[2 * t + 1];
+    const bool transposed = fabsf(c) > fabsf(s);   // uniform across the block
+    const float dyv = (float)jy - mid;
+    const float sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+    const float* base = (transposed ? PT : P) + (size_t)g * N * N * 8;
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    if (jy <= N) {
+        for (int jx = 1 + phase; jx <= N; jx += 4) {
+            const float dxv = (float)jx - mid;
+            const float xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
+            const float yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
+            const float x1f = floorf(xr), y1f = floorf(yr);
+            const int x1 = (int)x1f, y1 = (int)y1f;
+            if (min(x1, y1) > 1 && max(x1, y1) < N) {
+                const float wxl = add_rn(x1f, 1.f) - xr, wxh = xr - x1f;
+                const float wyl = add_rn(y1f, 1.f) - yr, wyh = yr - y1f;
+                const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
+                const float* p = transposed ? base + ((size_t)(x1 - 1) * N + (y1 - 1)) * 8
+                                            : base + ((size_t)(y1 - 1) * N + (x1 - 1)) * 8;
+                const Pair4 r0 = ld_pair(p);
+                const Pair4 r1 = ld_pair(p + (size_t)N * 8);
+                // normal: r0 = (x1,y1),(x1+1,y1)  r1 = (x1,y1+1),(x1+1,y1+1)
+                // transposed: r0 = (x1,y1),(x1,y1+1)  r1 = (x1+1,y1),(x1+1,y1+1)
+                const float wb0 = transposed ? w12 : w21;
+                const float wa1 = transposed ? w21 : w12;
+#pragma unroll
+                for (int v = 0; v < 4; ++v)
+                    acc[v] = fmaf(r1.b[v], w22, fmaf(r1.a[v], wa1, fmaf(r0.b[v], wb0, fmaf(r0.a[v], w11, acc[v]))));
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < 4; ++v) {
+        acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], 8);
+        acc[v] += __shfl_xor_sync(0xffffffffu, acc[v], 16);
+    }
+    if (phase == 0 && jy <= N) {
+        float4 o = make_float4(acc[0] / (float)N, acc[1] / (float)N, acc[2] / (float)N, acc[3] / (float)N);
+        *reinterpret_cast<float4*>(sino + (((size_t)g * T + t) * N + (jy - 1)) * 4) = o;
+    }
+}
+
+void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float* P, float* PT, float* sino,
+                        cudaStream_t st)
+{
+    dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
+    k_make_pairs<<<gp, bp, 0, st>>>(img, P, PT, g.N);
+    dim3 blk(32, 4), grd((g.N + 31) / 32, g.T, G);
+    k_radon_pairs<<<grd, blk, 0, st>>>(P, PT, g.sc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+}
+
+// ---------------------------------------------------------------------------
 // Exact transpose of k_radon, as a gather (no atomics, deterministic).  For
 // pixel (px,py) and angle theta the samples that use it as a bilinear tap lie
 // within sqrt(2) of its inverse-rotated position; each candidate sample is

@@ -180,6 +180,30 @@ class Tomography:
              fbp.ctypes.data_as(ctypes.c_void_p), ctx=self._h)
         return tv, fbp
 
+    # -- the batched solver in steps (device tensors) ------------------------------
+    def tv_begin(self, f, ninner: int, ncg: int, lam: float, mu: float, want_fbp: bool = False):
+        lead, S = self._shape_in(f, "sino")
+        if not (_is_cuda_tensor(f) and f.dtype == torch.float32):
+            raise TypeError("tv_begin takes a float32 CUDA tensor")
+        f = f.contiguous()
+        self._tv_shape = lead + (self.nimage, self.nimage)
+        self._tv_keep = f
+        fbp = torch.empty(self._tv_shape, dtype=f.dtype, device=f.device) if want_fbp else None
+        self._sync_stream()
+        call("acu_tv_begin", self._h, S, ctypes.c_void_p(f.data_ptr()), int(ninner), int(ncg), float(lam),
+             float(mu), ctypes.c_void_p(fbp.data_ptr()) if want_fbp else None, ctx=self._h)
+        return fbp
+
+    def tv_iterate(self, nouter: int):
+        self._sync_stream()
+        call("acu_tv_iterate", self._h, int(nouter), ctx=self._h)
+
+    def tv_end(self):
+        out = torch.empty(self._tv_shape, dtype=torch.float32, device="cuda")
+        self._sync_stream()
+        call("acu_tv_end", self._h, ctypes.c_void_p(out.data_ptr()), ctx=self._h)
+        return out
+
     def last_delta(self, nslices: int):
         out = np.zeros(nslices, np.float64)
         call("acu_tv_last_delta", self._h, int(nslices), out.ctypes.data_as(ctypes.c_void_p), ctx=self._h)

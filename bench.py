@@ -1,0 +1,356 @@
+"""Benchmark of the batched split-Bregman TV reconstruction (tomography/tv_hpc.F90
+tvopt) on GB300, following the repository's bench contract.
+
+Workload (one GPU): S = 256 slices of the 2049^2 grid (2048-pixel detector made
+odd, tv_hpc.F90:552-555) at T = 1200 angles over [0, 180] degrees, Bregman
+parameters ninner = 1, ncg = 10, lambda = 0.05, mu = 1.0, wpu = 100, nouter = 50.
+Inputs are seeded synthetic sinograms (random-ellipse phantoms, analytic
+projections, Poisson counts at I0 = 5e3): the reference's neutron-CT datasets
+are not available.
+
+A "step" is one Bregman outer iteration of the whole batch (10 CG steps: 11
+projector and 11 filtered-backprojection launches plus the fused element-wise
+kernels, replayed as one CUDA graph).  value = S / (t_warm + nouter * t_step):
+slices per second of the full 50-iteration reconstruction with the inputs
+resident in HBM (t_warm = the FBP warm start, timed once).  e2e = the same
+through the host-buffer C ABI call acu_tvopt (pinned host input and outputs,
+copies inside the timed region) for one outer iteration, plus the remaining
+nouter - 1 device-timed steps.
+
+--impl reference times the reference's algorithm on the host cores instead
+(the CPU oracle's single-precision restatement, every host thread), on a
+bounded sample of the same workload scaled to the same metric.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "TV slices/sec 2048²@1200 angles batched vs plain GPU at relL2≤1e-4; FBP GUPS"
+N_GRID, T_ANG, S_BATCH = 2049, 1200, 256
+NINNER, NCG, NOUTER, LAM, MU, WPU = 1, 10, 50, 0.05, 1.0, 100
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--slices", type=int, default=S_BATCH)
+    ap.add_argument("--size", type=int, default=N_GRID)
+    ap.add_argument("--angles", type=int, default=T_ANG)
+    ap.add_argument("--op", default=None, choices=[None, "radon", "iradon", "backproject", "filter", "tvstep"],
+                    help="time one operator on the workload's batch (used for ncu captures)")
+    ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--no-extras", action="store_true", help="skip e2e / plain / FBP / CPU legs")
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+        out = {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": len(self.rows)}
+        try:
+            sm = [float(r[0]) for r in self.rows if r[0] not in ("", "[N/A]")]
+            mx = [float(r[1]) for r in self.rows if r[1] not in ("", "[N/A]")]
+            if sm:
+                out["sm_mhz"] = statistics.median(sm)
+            if mx:
+                out["sm_max_mhz"] = max(mx)
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for i, n in enumerate(names):
+                if any(len(r) > 4 + i and r[4 + i].lower().startswith("active") for r in self.rows):
+                    out["reasons"].append(n)
+        except Exception:
+            pass
+        return out
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), "measured"
+    return 6800.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+def make_batch(S, N, T, device):
+    """S seeded synthetic sinograms (distinct phantoms for the first 16 slices,
+    repeated with a per-slice gain beyond that)."""
+    import torch
+    from acumen_gb300 import synthetic as syn
+    th = syn.angles(T, closed=True)
+    base = []
+    nbase = min(S, 16)
+    for s in range(nbase):
+        base.append(syn.normalised_sinogram(syn.random_ellipses(1000 + s, 0.35 * N), N, th, I0=5e3, seed=1000 + s,
+                                            device=device))
+    f = torch.empty(S, T, N, device=device, dtype=torch.float32)
+    for s in range(S):
+        f[s] = base[s % nbase] * (1.0 + 0.01 * (s // nbase))
+    return th, f
+
+
+def cuda_time(fn, reps, stream=None):
+    import torch
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record()
+    for _ in range(reps):
+        fn()
+    e1.record()
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / 1000.0 / reps
+
+
+# ---------------------------------------------------------------------------
+def cpu_reference_sample(N, T, threads=None, t_sample=24, nslices=None):
+    """The reference's algorithm on the host cores: the oracle's single-precision
+    radon + iradon (direct filter) of `nslices` slices (one per core, as the
+    reference's MPI ranks) on `t_sample` of the T angles.  Returns seconds of
+    one radon+iradon pair for that sample and the sample description."""
+    import numpy as np
+    from oracle import oracle as O
+    from acumen_gb300 import synthetic as syn
+    ncores = threads or os.cpu_count() or 1
+    ns = nslices or ncores
+    th = syn.angles(T, closed=True)[:: max(1, T // t_sample)][:t_sample]
+    rng = np.random.default_rng(0)
+    img = rng.random((ns, N, N), dtype=np.float32)
+    sino = rng.random((ns, len(th), N), dtype=np.float32)
+    O.lib()
+    t0 = time.perf_counter()
+    O.radon(img, th, 32)
+    t1 = time.perf_counter()
+    O.iradon(sino, th, WPU, 32)
+    t2 = time.perf_counter()
+    desc = (f"oracle single-precision radon + iradon (direct filter) of {ns} slices of {N}^2 on "
+            f"{len(th)} of {T} angles, OpenMP over {ncores} threads; scaled by T/{len(th)} and by "
+            f"the reference's {NCG + 2} radon + {NCG + 2} iradon per outer iteration")
+    return (t1 - t0), (t2 - t1), len(th), ns, ncores, desc
+
+
+def cpu_slices_per_s(N, T, threads=None):
+    tr, ti, ts, ns, ncores, desc = cpu_reference_sample(N, T, threads)
+    scale = T / ts
+    t_outer = (NCG + 2) * (tr + ti) * scale          # ns slices in parallel
+    t_job = NOUTER * t_outer + ti * scale           # + FBP warm start
+    return ns / t_job, ncores, desc
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, ncores, desc = cpu_slices_per_s(args.size, args.angles)
+        if i >= args.warmup:
+            vals.append(v)
+    v = statistics.median(vals)
+    line = {"metric": METRIC, "value": v, "unit": "slices/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * args.slices / v / NOUTER, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "impl": "reference",
+            "config": {"workload": f"split-Bregman TV, {args.slices} slices of {args.size}^2, {args.angles} angles, "
+                                   f"ninner={NINNER} ncg={NCG} nouter={NOUTER} lambda={LAM} mu={MU} wpu={WPU}",
+                       "global_batch": args.slices, "parallelism": "host threads"},
+            "cpu_baseline": {"value": v, "unit": "slices/s", "cores": ncores, "kind": "port", "sample": desc},
+            "e2e": {"value": v, "unit": "slices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_op(args, t, f, S):
+    """One operator on the batch, for ncu captures and kernel timings."""
+    import torch
+    N = args.size
+    if args.op == "radon":
+        img = torch.rand(S, N, N, device="cuda")
+        fn = lambda: t.radon(img)
+    elif args.op == "iradon":
+        fn = lambda: t.iradon(f)
+    elif args.op == "backproject":
+        fn = lambda: t.backproject(f)
+    elif args.op == "filter":
+        fn = lambda: t.filter(f)
+    else:
+        t.tv_begin(f, NINNER, NCG, LAM, MU)
+        fn = lambda: t.tv_iterate(1)
+    for _ in range(args.warmup):
+        fn()
+    sec = cuda_time(fn, args.reps)
+    print(json.dumps({"op": args.op, "slices": S, "N": N, "T": args.angles, "ms": 1000 * sec}), flush=True)
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+
+    import numpy as np
+    import torch
+    import torch.distributed as dist
+    from acumen_gb300 import build as _build
+    from acumen_gb300.tomography import Tomography
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+    _build.build()
+    N, T, S = args.size, args.angles, args.slices
+    th, f = make_batch(S, N, T, "cuda")
+    t = Tomography(N, th, WPU)
+    if args.op:
+        return run_op(args, t, f, S)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    # warm start (FBP + initialisation), timed once
+    barrier()
+    t_warm = cuda_time(lambda: t.tv_begin(f, NINNER, NCG, LAM, MU), 1)
+    for _ in range(args.warmup):
+        t.tv_iterate(1)
+    barrier()
+    sampler = ClockSampler(local)
+    sampler.start()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record()
+    for _ in range(args.steps):
+        t.tv_iterate(1)
+    e1.record()
+    torch.cuda.synchronize()
+    clocks = sampler.stop()
+    t_step = e0.elapsed_time(e1) / 1000.0 / args.steps
+    if world > 1:
+        tt = torch.tensor([t_step, t_warm], device="cuda", dtype=torch.float64)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_step, t_warm = tt.tolist()
+    t_job = t_warm + NOUTER * t_step
+    value = world * S / t_job
+    # kernels of one outer iteration (the captured graph): projector launches,
+    # filter + backprojection per iradon, and the element-wise / finaliser kernels
+    n_radon = NINNER * NCG + (NINNER - 1) + 1
+    n_iradon = NINNER * (2 + NCG)
+    n_ew = NINNER * (4 + 5 * NCG) + 1
+    kernel_launches = n_radon + 2 * n_iradon + n_ew
+
+    line = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random-ellipse phantoms, Poisson I0=5e3)",
+            "config": {"workload": f"split-Bregman TV, {S} slices of {N}^2, {T} angles over [0,180], "
+                                   f"ninner={NINNER} ncg={NCG} nouter={NOUTER} lambda={LAM} mu={MU} wpu={WPU}; "
+                                   f"step = one outer iteration of the batch",
+                       "global_batch": S * world, "seq_len": T, "parallelism": f"slices sharded, {world} rank(s)",
+                       "l2": "inputs larger than L2 (batch state > 50 GB)",
+                       "t_warm_s": t_warm, "t_step_s": t_step},
+            "clocks": clocks, "gpu_launches": kernel_launches * args.steps}
+
+    if rank == 0 and not args.no_extras:
+        # dominant kernel: the projector, timed alone on the same batch (lane layout, 64 slice groups)
+        img = torch.rand(S, N, N, device="cuda")
+        t_radon = cuda_time(lambda: t.radon(img), 2)
+        del img
+        hbm, kind = measured_peaks()
+        alg_bytes = 4.0 * (N * N + N * T) * S
+        achieved = alg_bytes / t_radon / 1e9
+        line["roofline"] = {"bound": "hbm", "kernel": "k_radon (projector, tv_hpc.F90:137-156)",
+                            "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                            "peak_kind": kind, "traffic": None,
+                            "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,
+                            "l1_level_GBps": 16.0 * N * N * T * S / t_radon / 1e9,
+                            "samples_per_s": N * N * T * S / t_radon}
+        # end to end through the host-buffer C ABI: one outer iteration with copies
+        fh = f.cpu().pin_memory()
+        tvh = torch.empty(S, N, N, pin_memory=True)
+        fbph = torch.empty(S, N, N, pin_memory=True)
+        import ctypes
+        from acumen_gb300._lib import call
+
+        def e2e_call():
+            call("acu_tvopt", t.handle, S, ctypes.c_void_p(fh.data_ptr()), NINNER, 1, NCG, LAM, MU,
+                 ctypes.c_void_p(tvh.data_ptr()), ctypes.c_void_p(fbph.data_ptr()), ctx=t.handle)
+        e2e_call()
+        t0 = time.perf_counter()
+        e2e_call()
+        t_e2e1 = time.perf_counter() - t0
+        e2e_val = S / (t_e2e1 + (NOUTER - 1) * t_step)
+        line["e2e"] = {"value": e2e_val, "unit": "slices/s", "h2d_bytes_per_step": 4 * S * T * N,
+                       "d2h_bytes_per_step": 2 * 4 * S * N * N,
+                       "how": "acu_tvopt host call (pinned in, tv+fbp out, FBP + 1 outer iteration) "
+                              f"= {t_e2e1:.3f} s, plus {NOUTER - 1} device-timed steps"}
+        del fh, tvh, fbph
+        # the plain per-slice GPU path (reference structure) on one slice
+        f1 = f[:1].contiguous()
+        tp1 = cuda_time(lambda: t.tvopt(f1, NINNER, 1, NCG, LAM, MU, plain=True), 1)
+        tp2 = cuda_time(lambda: t.tvopt(f1, NINNER, 2, NCG, LAM, MU, plain=True), 1)
+        t_plain_outer = max(tp2 - tp1, 1e-9)
+        plain_val = 1.0 / (tp1 - t_plain_outer + NOUTER * t_plain_outer)
+        line["plain_gpu"] = {"value": plain_val, "unit": "slices/s", "outer_s_per_slice": t_plain_outer,
+                             "batched_over_plain": value / plain_val}
+        # FBP GUPS: config 1 single slice (725^2, 720 angles) and the batch
+        from acumen_gb300 import synthetic as syn
+        t1c = Tomography(725, syn.angles(720), WPU)
+        s1 = torch.rand(1, 720, 725, device="cuda")
+        g1 = 725 * 725 * 720 / cuda_time(lambda: t1c.iradon(s1), 10) / 1e9
+        gb = N * N * T * S / cuda_time(lambda: t.iradon(f), 2) / 1e9
+        line["fbp_gups"] = {"config1_single_slice": g1, "batch_2049sq_1200_x256": gb}
+        # CPU baseline (bounded sample, all host cores)
+        v, ncores, desc = cpu_slices_per_s(N, T)
+        line["cpu_baseline"] = {"value": v, "unit": "slices/s", "cores": ncores, "kind": "port", "sample": desc}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -107,9 +107,81 @@ int acu_tvopt_plain_dev(acu_ctx *ctx, int nslices, const float *d_f, int ninner,
                         int ncg, float lambda, float mu, float *d_tv, float *d_fbp);
 int acu_tvopt_dev_f64(acu_ctx *ctx, int nslices, const double *d_f, int ninner, int nouter,
                       int ncg, double lambda, double mu, double *d_tv, double *d_fbp);
+/* The batched solver in steps, for callers that interleave their own work or
+ * time the outer iterations: acu_tv_begin = allocation, copy of d_f (S*T*N,
+ * device) and the warm start of tv_hpc.F90:172-202 (FBP into d_fbp when not
+ * NULL); acu_tv_iterate = nouter more outer iterations of tv_hpc.F90:205-353
+ * (callable repeatedly; the iteration is captured once as a CUDA graph);
+ * acu_tv_end = copy of the current TV iterate to d_tv (S*N*N, device).
+ * acu_tvopt_dev is begin + iterate(nouter) + end.                            */
+int acu_tv_begin(acu_ctx *ctx, int nslices, const float *d_f, int ninner, int ncg, float lambda,
+                 float mu, float *d_fbp);
+int acu_tv_iterate(acu_ctx *ctx, int nouter);
+int acu_tv_end(acu_ctx *ctx, float *d_tv);
 /* Print-only Err_diff of the last outer iteration per slice (tv_hpc.F90:327-333),
  * available after a tvopt call with ACU_OPT_VERBOSE set.                     */
 int acu_tv_last_delta(const acu_ctx *ctx, int nslices, double *delta);
+
+/* ---- projection preprocessing (device pointers, ordered on ctx's stream) ----
+ * Any context works, including one created with nimage = 0.  Projections are
+ * ndet x nrows floats with the detector fastest (the reference's square
+ * nimage x nimage projections generalised to ndet != nrows); a stack holds
+ * nproj of them.  Angles are host arrays in degrees.
+ *
+ * acu_frame_average*: tomography/fits_to_hpc.F90:183-210 -- mean of a stack
+ *   of open-beam (flat) or dark frames, summed in frame order.
+ * acu_normalize*: fits_to_hpc.F90:243 (mode 0: -log(I / max(OB,1)), the
+ *   reference's active line) and :244 (mode 1: -log(max(I-DF,1e-16) /
+ *   max(OB-DF,1)), its flat/dark alternative), for nproj projections.
+ * acu_pick_angle_dev: projections_to_sinogram_hpc.F90:141-224 -- the
+ *   projection at exactly `target` degrees (0 or 180): the nearest one when
+ *   it lies at the target or has no neighbour across it, else the linear
+ *   interpolation of the two projections bracketing the target.
+ * acu_register_dev: :231-364 -- centre-of-mass initial shift and the
+ *   multiplicative pattern search over (tilt, shift) minimising the mirrored
+ *   L1 mismatch of the resampled 0/180-degree projections.  theta in radians,
+ *   shift as a fraction of ndet, as the reference.
+ * acu_xcorr_register_dev: new -- integer lag k maximising the correlation of
+ *   the 0-degree projection with the mirrored 180-degree one over
+ *   k = -kmax..kmax (products summed as 2^-32 fixed point, so the integer lag is
+ *   bit-exact and independent of summation order; ties go to the lowest k),
+ *   and the parabolic sub-pixel vertex k_sub.  The axis sits at detector
+ *   position (ndet - 1 + k_sub)/2 (0-based); the equivalent reference shift
+ *   is (add - k_sub) / (2 ndet), add = 1 for even ndet.
+ * acu_median27_dev: :426-452 -- median of the 3x3 neighbourhood (clamped) in
+ *   the previous, current and next projection, with the intended slots 1..27
+ *   (the reference's slot expression indexes -2..24).
+ * acu_resample_dev: :456-470 -- bilinear resample onto the (ndet+add) x nrows
+ *   grid under (theta, shift), with the reference's clamps.
+ * acu_proj_to_sino_dev: :397-487 -- median, resample and transpose of every
+ *   projection into nrows sinograms of nproj x (ndet+add) (slice-major:
+ *   sino[row][projection][det]).
+ * acu_proj_to_sino_u16: the whole chain on host buffers: raw uint16
+ *   projections, flat and dark stacks -> averages -> normalisation (norm_mode)
+ *   -> 0/180 picks -> registration (reg_method 0: the reference's pattern
+ *   search, 1: cross-correlation) -> median, resample, transpose.            */
+int acu_frame_average_u16_dev(acu_ctx *ctx, int nframes, long npix, const uint16_t *d_frames, float *d_out);
+int acu_frame_average_dev(acu_ctx *ctx, int nframes, long npix, const float *d_frames, float *d_out);
+int acu_normalize_u16_dev(acu_ctx *ctx, int mode, int nproj, long npix, const uint16_t *d_raw,
+                          const float *d_ob, const float *d_df, float *d_out);
+int acu_normalize_dev(acu_ctx *ctx, int mode, int nproj, long npix, const float *d_raw, const float *d_ob,
+                      const float *d_df, float *d_out);
+int acu_pick_angle_dev(acu_ctx *ctx, int nfiles, const float *theta_deg, long npix, const float *d_proj,
+                       float target, float *d_out);
+int acu_register_dev(acu_ctx *ctx, int ndet, int nrows, const float *d_p0, const float *d_p180,
+                     float *theta_out, float *shift_out, int *evals_out);
+int acu_xcorr_register_dev(acu_ctx *ctx, int ndet, int nrows, const float *d_p0, const float *d_p180,
+                           int kmax, int64_t *corr_out, int *k_best, double *k_sub);
+int acu_median27_dev(acu_ctx *ctx, int ndet, int nrows, const float *d_l, const float *d_c, const float *d_r,
+                     float *d_out);
+int acu_resample_dev(acu_ctx *ctx, int ndet, int nrows, const float *d_src, float theta, float shift,
+                     float *d_out);
+int acu_proj_to_sino_dev(acu_ctx *ctx, int nproj, int ndet, int nrows, const float *d_proj, float theta,
+                         float shift, float *d_sino);
+int acu_proj_to_sino_u16(acu_ctx *ctx, int nproj, int ndet, int nrows, const uint16_t *raw,
+                         const float *theta_deg, int nflat, const uint16_t *flats, int ndark,
+                         const uint16_t *darks, int norm_mode, int reg_method, float *sino_out,
+                         float *theta_out, float *shift_out);
 
 #ifdef __cplusplus
 }
