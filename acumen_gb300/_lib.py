@@ -80,6 +80,7 @@ SIGNATURES = {
     "acu_resample_dev": [P, I, I, P, F, F, P],
     "acu_proj_to_sino_dev": [P, I, I, I, P, F, F, P],
     "acu_proj_to_sino_u16": [P, I, I, I, P, P, I, P, I, P, I, I, P, P, P],
+    "acu_xcorr_register_noalloc": [I, I, P, P, I, P, P, P, P],
 }
 
 

@@ -183,6 +183,25 @@ int acu_proj_to_sino_u16(acu_ctx *ctx, int nproj, int ndet, int nrows, const uin
                          const uint16_t *darks, int norm_mode, int reg_method, float *sino_out,
                          float *theta_out, float *shift_out);
 
+/* ---- cross-correlation registration without device allocation --------------
+ * No counterpart in the reference.  Same computation and results as
+ * acu_xcorr_register_dev, for callers that must not have the library allocate
+ * device memory (device memory reserved up front by an acquisition pipeline
+ * or owned by another allocator, or a thread that cannot afford the implicit
+ * synchronisation of cudaMalloc/cudaFree).  It needs no context: its scratch
+ * is a fixed array inside the library, 2*2048+3 eight-byte words, present on
+ * every GPU that loads the library until the process exits, so kmax is
+ * limited to 1..2048 (larger kmax returns ACU_ERR_INVALID).  The first call on
+ * a device resolves that array's device address (cudaGetSymbolAddress) with
+ * the device current; make that first call before any stream capture.  All
+ * calls share the one array: each call clears the sums it uses before
+ * accumulating, and calls whose work overlaps on the GPU (other streams,
+ * other host threads) race on it -- serialise them.  The work is ordered on
+ * `stream` (NULL: the legacy default stream); the call returns after the
+ * results are read back.  Errors are reported by acu_last_error(NULL).      */
+int acu_xcorr_register_noalloc(int ndet, int nrows, const float *d_p0, const float *d_p180, int kmax,
+                               int64_t *corr_out, int *k_best, double *k_sub, void *stream);
+
 #ifdef __cplusplus
 }
 #endif
