@@ -567,6 +567,51 @@ int tv_host(acu_ctx* c, bool plain, int S, const float* f, int ninner, int noute
 
 }  // namespace
 
+// ---- registration-aware TV objective and its gradient (new) -------------------
+template <typename Real>
+int tv_loss_grad(acu_ctx* c, int S, const Real* d_u, const Real* d_off, const Real* d_y, double lambda, double eps,
+                 double* loss_out, Real* d_grad_u, Real* d_grad_off)
+{
+    CKRET(check_ctx(c, S));
+    if (S == 0) return ACU_OK;
+    if (!d_u || !d_y || !loss_out) return set_err(c, ACU_ERR_INVALID, "null array");
+    if (!(eps > 0.0)) return set_err(c, ACU_ERR_INVALID, "eps must be > 0 (smoothed total variation)");
+    CKRET(ensure_geom<Real>(c));
+    const DevGeom<Real>& g = geomset<Real>(c).d;
+    const int N = c->N, T = c->T;
+    const size_t nsino = (size_t)T * N, nimg = (size_t)N * N;
+    const int nblk = (int)std::min<size_t>((nimg + 255) / 256, 512);
+    CK(c, c->w_in.ensure(sizeof(Real) * nsino * S));      // residual
+    CK(c, c->w_out.ensure(sizeof(Real) * nsino * S));     // offset derivative of the projector
+    CK(c, c->w_part.ensure(sizeof(double) * ((size_t)2 * nblk * S + 2 * S)));
+    Real* r = c->w_in.template as<Real>();
+    Real* D = c->w_out.template as<Real>();
+    double* part = c->w_part.template as<double>();
+    double* sums = part + (size_t)2 * nblk * S;
+    cudaStream_t st = c->stream;
+    launch_radon_off<Real>(g, S, d_u, d_off, r, st);
+    GradEw<Real>::residual(nsino, S, r, d_y, part, nblk, st);
+    launch_sum_rows(part, S, nblk, sums, st);
+    Real* gu = d_grad_u;
+    if (!gu) {
+        CK(c, c->w_q.ensure(sizeof(Real) * nimg * S));
+        gu = c->w_q.template as<Real>();
+    }
+    launch_radon_adjoint_off<Real>(g, S, r, d_off, gu, st);
+    GradEw<Real>::tv_grad(N, S, (Real)lambda, (Real)eps, d_u, gu, part + (size_t)nblk * S, nblk, st);
+    launch_sum_rows(part + (size_t)nblk * S, S, nblk, sums + S, st);
+    if (d_grad_off) {
+        launch_radon_doff<Real>(g, S, d_u, d_off, D, st);
+        GradEw<Real>::off_grad(N, T, S, r, D, d_grad_off, st);
+    }
+    CKLAUNCH(c);
+    std::vector<double> h(2 * (size_t)S);
+    CK(c, cudaMemcpyAsync(h.data(), sums, sizeof(double) * 2 * S, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    for (int k = 0; k < S; ++k) loss_out[k] = h[k] + h[S + k];
+    return ACU_OK;
+}
+
 // =============================================================================
 // exported C ABI
 // =============================================================================
@@ -712,6 +757,17 @@ int acu_tv_begin(acu_ctx* c, int S, const float* d_f, int ninner, int ncg, float
 }
 int acu_tv_iterate(acu_ctx* c, int nouter) { return tv_iterate<float>(c, nouter); }
 int acu_tv_end(acu_ctx* c, float* d_tv) { return tv_end<float>(c, d_tv); }
+
+int acu_tv_loss_grad_dev(acu_ctx* c, int S, const float* d_u, const float* d_off, const float* d_y, float lambda,
+                         float eps, double* loss, float* d_grad_u, float* d_grad_off)
+{
+    return tv_loss_grad<float>(c, S, d_u, d_off, d_y, lambda, eps, loss, d_grad_u, d_grad_off);
+}
+int acu_tv_loss_grad_dev_f64(acu_ctx* c, int S, const double* d_u, const double* d_off, const double* d_y,
+                             double lambda, double eps, double* loss, double* d_grad_u, double* d_grad_off)
+{
+    return tv_loss_grad<double>(c, S, d_u, d_off, d_y, lambda, eps, loss, d_grad_u, d_grad_off);
+}
 
 int acu_tv_last_delta(const acu_ctx* c, int S, double* delta)
 {

@@ -42,6 +42,28 @@ void launch_filter_fft(const DevGeom<Real>& g, int G, const Real* sino, Real* ou
 template <typename Real>
 bool fft_fits(int L);
 
+// ---- projector / adjoint with per-slice, per-angle detector offsets off[S][T]
+// (plain layout, one slice per thread) and the offset derivative of the
+// projector (kernels_radon.cu); the loss / gradient steps (kernels_grad.cu).
+template <typename Real>
+void launch_radon_off(const DevGeom<Real>& g, int S, const Real* img, const Real* off, Real* sino, cudaStream_t st);
+template <typename Real>
+void launch_radon_adjoint_off(const DevGeom<Real>& g, int S, const Real* sino, const Real* off, Real* img,
+                              cudaStream_t st);
+template <typename Real>
+void launch_radon_doff(const DevGeom<Real>& g, int S, const Real* img, const Real* off, Real* dsino, cudaStream_t st);
+template <typename Real>
+struct GradEw {
+    // r = A u - y in place (r holds A u), per-slice FP64 partials of 1/2 |r|^2
+    static void residual(size_t n_per, int S, Real* r, const Real* y, double* part, int nblk, cudaStream_t st);
+    // grad_u += lambda * dTV_eps/du; per-slice partials of lambda * TV_eps(u)
+    static void tv_grad(int N, int S, Real lambda, Real eps, const Real* u, Real* grad, double* part, int nblk,
+                        cudaStream_t st);
+    // grad_off[s][t] = sum_jy r * D
+    static void off_grad(int N, int T, int S, const Real* r, const Real* D, Real* grad_off, cudaStream_t st);
+};
+void launch_sum_rows(const double* part, int rows, int nblk, double* out, cudaStream_t st);
+
 // ---- layout conversion (kernels_tv.cu) ------------------------------------
 // plain [S][npos] <-> lanes [G][npos][V]; slices >= S of the last group are 0.
 template <typename Real, int V>

@@ -76,14 +76,16 @@ void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img,
 // ---------------------------------------------------------------------------
 template <typename Real, int V>
 __global__ void __launch_bounds__(128) k_radon(const Real* __restrict__ img, const Real* __restrict__ sc,
-                                               Real* __restrict__ sino, int N, int T, Real mid)
+                                               Real* __restrict__ sino, int N, int T, Real mid,
+                                               const Real* __restrict__ off)
 {
     const int jy = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int t = blockIdx.y * blockDim.y + threadIdx.y;
     const int g = blockIdx.z;
     if (jy > N || t >= T) return;
     const Real s = sc[2 * t], c = sc[2 * t + 1];
-    const Real dyv = (Real)jy - mid;
+    // bin jy is read at detector coordinate jy + off[t] (off: per-slice angle offsets, V = 1)
+    const Real dyv = off ? sub_rn(add_rn((Real)jy, off[(size_t)g * T + t]), mid) : (Real)jy - mid;
     const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
     const Real* u = img + (size_t)g * N * N * V;
     const size_t rowstride = (size_t)N * V;
@@ -119,7 +121,7 @@ template <typename Real, int V>
 void launch_radon(const DevGeom<Real>& g, int G, const Real* img, Real* sino, cudaStream_t st)
 {
     dim3 blk(32, 4), grd((g.N + 31) / 32, (g.T + 3) / 4, G);
-    k_radon<Real, V><<<grd, blk, 0, st>>>(img, g.sc_fp, sino, g.N, g.T, g.mid);
+    k_radon<Real, V><<<grd, blk, 0, st>>>(img, g.sc_fp, sino, g.N, g.T, g.mid, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -263,7 +265,8 @@ void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float*
 template <typename Real, int V>
 __global__ void __launch_bounds__(256) k_radon_adjoint(const Real* __restrict__ sino,
                                                        const Real* __restrict__ sc,
-                                                       Real* __restrict__ img, int N, int T, Real mid)
+                                                       Real* __restrict__ img, int N, int T, Real mid,
+                                                       const Real* __restrict__ off)
 {
     const int px = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int py = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -280,14 +283,15 @@ __global__ void __launch_bounds__(256) k_radon_adjoint(const Real* __restrict__ 
             const Lanes<Real, 2> scp = ld_lanes<Real, 2>(sc + 2 * t);
             const Real s = scp.v[0], c = scp.v[1];
             // tap (px,py) of a sample at (xr,yr) means xr in [px-1,px+1), yr in [py-1,py+1)
+            const Real o = off ? off[(size_t)g * T + t] : Real(0);
             const Real u = c * ex + s * ey + mid;       // jx of the sample at the pixel
-            const Real w = -s * ex + c * ey + mid;      // jy
+            const Real w = -s * ex + c * ey + mid - o;  // jy
             int jx0 = (int)rfloor(u - Real(1.5)), jx1 = (int)rfloor(u + Real(1.5)) + 1;
             int jy0 = (int)rfloor(w - Real(1.5)), jy1 = (int)rfloor(w + Real(1.5)) + 1;
             jx0 = max(jx0, 1); jy0 = max(jy0, 1); jx1 = min(jx1, N); jy1 = min(jy1, N);
             const Real* yt = yg + (size_t)t * N * V;
             for (int jy = jy0; jy <= jy1; ++jy) {
-                const Real dyv = (Real)jy - mid;
+                const Real dyv = off ? sub_rn(add_rn((Real)jy, o), mid) : (Real)jy - mid;
                 const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
                 Real wsum = Real(0);
                 for (int jx = jx0; jx <= jx1; ++jx) {
@@ -320,7 +324,7 @@ template <typename Real, int V>
 void launch_radon_adjoint(const DevGeom<Real>& g, int G, const Real* sino, Real* img, cudaStream_t st)
 {
     dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G);
-    k_radon_adjoint<Real, V><<<grd, blk, 0, st>>>(sino, g.sc_fp, img, g.N, g.T, g.mid);
+    k_radon_adjoint<Real, V><<<grd, blk, 0, st>>>(sino, g.sc_fp, img, g.N, g.T, g.mid, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -382,6 +386,72 @@ void launch_filter_direct(const DevGeom<Real>& g, int G, const Real* sino, Real*
     dim3 grd(g.T, G);
     k_filter_direct<Real, V, RB><<<grd, 256, sm, st>>>(sino, g.filt, out, g.N, g.T);
 }
+
+// ---- projector with per-angle detector offsets and its derivatives ------------
+template <typename Real>
+void launch_radon_off(const DevGeom<Real>& g, int S, const Real* img, const Real* off, Real* sino, cudaStream_t st)
+{
+    dim3 blk(32, 4), grd((g.N + 31) / 32, (g.T + 3) / 4, S);
+    k_radon<Real, 1><<<grd, blk, 0, st>>>(img, g.sc_fp, sino, g.N, g.T, g.mid, off);
+}
+template <typename Real>
+void launch_radon_adjoint_off(const DevGeom<Real>& g, int S, const Real* sino, const Real* off, Real* img,
+                              cudaStream_t st)
+{
+    dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, S);
+    k_radon_adjoint<Real, 1><<<grd, blk, 0, st>>>(sino, g.sc_fp, img, g.N, g.T, g.mid, off);
+}
+
+// D(jy,theta) = d/d(off) of the projector's value: (1/N) sum_jx of the
+// bilinear gradient along the detector direction, dB/dx * (-sin) + dB/dy * cos.
+template <typename Real>
+__global__ void __launch_bounds__(128) k_radon_doff(const Real* __restrict__ img, const Real* __restrict__ sc,
+                                                    Real* __restrict__ dsino, int N, int T, Real mid,
+                                                    const Real* __restrict__ off)
+{
+    const int jy = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int t = blockIdx.y * blockDim.y + threadIdx.y;
+    const int g = blockIdx.z;
+    if (jy > N || t >= T) return;
+    const Real s = sc[2 * t], c = sc[2 * t + 1];
+    const Real dyv = off ? sub_rn(add_rn((Real)jy, off[(size_t)g * T + t]), mid) : (Real)jy - mid;
+    const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+    const Real* u = img + (size_t)g * N * N;
+    Real acc = Real(0);
+    for (int jx = 1; jx <= N; ++jx) {
+        const Real dxv = (Real)jx - mid;
+        const Real xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
+        const Real yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
+        const Real x1f = rfloor(xr), y1f = rfloor(yr);
+        const int x1 = (int)x1f, y1 = (int)y1f;
+        if (min(x1, y1) > 1 && max(x1, y1) < N) {
+            const Real wxl = add_rn(x1f, Real(1)) - xr, wxh = xr - x1f;
+            const Real wyl = add_rn(y1f, Real(1)) - yr, wyh = yr - y1f;
+            const Real* p = u + (size_t)(y1 - 1) * N + (x1 - 1);
+            const Real a = p[0], b = p[1], cc = p[N], d = p[N + 1];
+            const Real gx = (b - a) * wyl + (d - cc) * wyh;
+            const Real gy = (cc - a) * wxl + (d - b) * wxh;
+            acc += gy * c - gx * s;
+        }
+    }
+    dsino[((size_t)g * T + t) * N + (jy - 1)] = acc / (Real)N;
+}
+template <typename Real>
+void launch_radon_doff(const DevGeom<Real>& g, int S, const Real* img, const Real* off, Real* dsino, cudaStream_t st)
+{
+    dim3 blk(32, 4), grd((g.N + 31) / 32, (g.T + 3) / 4, S);
+    k_radon_doff<Real><<<grd, blk, 0, st>>>(img, g.sc_fp, dsino, g.N, g.T, g.mid, off);
+}
+template void launch_radon_off<float>(const DevGeom<float>&, int, const float*, const float*, float*, cudaStream_t);
+template void launch_radon_off<double>(const DevGeom<double>&, int, const double*, const double*, double*,
+                                       cudaStream_t);
+template void launch_radon_adjoint_off<float>(const DevGeom<float>&, int, const float*, const float*, float*,
+                                              cudaStream_t);
+template void launch_radon_adjoint_off<double>(const DevGeom<double>&, int, const double*, const double*, double*,
+                                               cudaStream_t);
+template void launch_radon_doff<float>(const DevGeom<float>&, int, const float*, const float*, float*, cudaStream_t);
+template void launch_radon_doff<double>(const DevGeom<double>&, int, const double*, const double*, double*,
+                                        cudaStream_t);
 
 // ---- explicit instantiations ------------------------------------------------
 #define ACU_INST(R, V)                                                                          \

@@ -204,6 +204,30 @@ class Tomography:
         call("acu_tv_end", self._h, ctypes.c_void_p(out.data_ptr()), ctx=self._h)
         return out
 
+    def tv_loss_grad(self, u, off, y, lam: float, eps: float, want_grad: bool = True):
+        """Registration-aware TV objective (new): returns (loss[S] float64 numpy,
+        grad_u, grad_off) for CUDA tensors u[S,N,N], off[S,T] (or None),
+        y[S,T,N]; float64 tensors use the double-precision kernels."""
+        lead, S = self._shape_in(u, "img")
+        if not (_is_cuda_tensor(u) and _is_cuda_tensor(y)):
+            raise TypeError("tv_loss_grad takes CUDA tensors")
+        dt = u.dtype
+        u, y = u.contiguous(), y.contiguous().to(dt)
+        offp = None
+        if off is not None:
+            off = off.contiguous().to(dt)
+            offp = ctypes.c_void_p(off.data_ptr())
+        gu = torch.empty_like(u) if want_grad else None
+        go = torch.empty(lead + (self.ntheta,), dtype=dt, device=u.device) if (want_grad and off is not None) else None
+        loss = np.zeros(S, np.float64)
+        self._sync_stream()
+        fn = "acu_tv_loss_grad_dev_f64" if dt == torch.float64 else "acu_tv_loss_grad_dev"
+        call(fn, self._h, S, ctypes.c_void_p(u.data_ptr()), offp, ctypes.c_void_p(y.data_ptr()), float(lam),
+             float(eps), loss.ctypes.data_as(ctypes.c_void_p),
+             ctypes.c_void_p(gu.data_ptr()) if gu is not None else None,
+             ctypes.c_void_p(go.data_ptr()) if go is not None else None, ctx=self._h)
+        return loss.reshape(lead) if lead else loss[0], gu, go
+
     def last_delta(self, nslices: int):
         out = np.zeros(nslices, np.float64)
         call("acu_tv_last_delta", self._h, int(nslices), out.ctypes.data_as(ctypes.c_void_p), ctx=self._h)

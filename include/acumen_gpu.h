@@ -118,6 +118,21 @@ int acu_tv_begin(acu_ctx *ctx, int nslices, const float *d_f, int ninner, int nc
                  float mu, float *d_fbp);
 int acu_tv_iterate(acu_ctx *ctx, int nouter);
 int acu_tv_end(acu_ctx *ctx, float *d_tv);
+/* ---- registration-aware TV objective and its gradient (new) -----------------
+ * For S slices with per-angle detector offsets off[S][T] (pixels; NULL = 0):
+ *   loss[s] = 1/2 |A_off u - y|^2 + lambda * sum_i sqrt((Dx u)_i^2 + eps^2)
+ *                                            + sqrt((Dy u)_i^2 + eps^2)
+ * A_off is the projector of tv_hpc.F90:137-156 with bin jy read at detector
+ * coordinate jy + off[t] (off = 0 is acu_radon exactly); Dx, Dy are the
+ * periodic backward differences of the shrinkage step (tv_hpc.F90:305-325).
+ * Writes loss (host, S doubles), d_grad_u (S*N*N) = A_off^T r + lambda
+ * dTV/du, computed with the exact adjoint, and d_grad_off (S*T) = the
+ * derivative with respect to each angle's offset (either may be NULL).     */
+int acu_tv_loss_grad_dev(acu_ctx *ctx, int nslices, const float *d_u, const float *d_off, const float *d_y,
+                         float lambda, float eps, double *loss, float *d_grad_u, float *d_grad_off);
+int acu_tv_loss_grad_dev_f64(acu_ctx *ctx, int nslices, const double *d_u, const double *d_off,
+                             const double *d_y, double lambda, double eps, double *loss, double *d_grad_u,
+                             double *d_grad_off);
 /* Print-only Err_diff of the last outer iteration per slice (tv_hpc.F90:327-333),
  * available after a tvopt call with ACU_OPT_VERBOSE set.                     */
 int acu_tv_last_delta(const acu_ctx *ctx, int nslices, double *delta);
