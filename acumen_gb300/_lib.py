@@ -81,6 +81,8 @@ SIGNATURES = {
     "acu_proj_to_sino_dev": [P, I, I, I, P, F, F, P],
     "acu_proj_to_sino_u16": [P, I, I, I, P, P, I, P, I, P, I, I, P, P, P],
     "acu_xcorr_register_noalloc": [I, I, P, P, I, P, P, P, P],
+    "acu_normalize_stack_u16": [P, I, I, L, P, I, P, I, P, P],
+    "acu_proj_to_sino": [P, I, I, I, P, P, I, P, P, P],
     "acu_tv_loss_grad_dev": [P, I, P, P, P, F, F, P, P, P],
     "acu_tv_loss_grad_dev_f64": [P, I, P, P, P, D, D, P, P, P],
 }

@@ -62,6 +62,34 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     return OUT
 
 
+DRIVERS = ["raw_to_hpc", "projections_to_sinogram_hpc", "fbp_hpc", "tv_hpc", "tv_hpc_slice"]
+BIN = os.path.join(HERE, "bin")
+
+
+def build_drivers(force: bool = False) -> list:
+    """The C++ drop-ins for the reference's driver programs, linked against
+    libacumen_gpu.so (found next to the package through the rpath)."""
+    lib = build(force)
+    os.makedirs(BIN, exist_ok=True)
+    cxx = os.environ.get("CXX", "g++")
+    out = []
+    def one(name):
+        src = os.path.join(HERE, "drivers", name + ".cpp")
+        exe = os.path.join(BIN, name)
+        deps = [src, os.path.join(HERE, "drivers", "hpc_io.h"), lib]
+        if force or not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
+            cmd = [cxx, "-O2", "-std=c++17", "-Wall", src, "-o", exe, "-L" + HERE, "-lacumen_gpu",
+                   "-Wl,-rpath,$ORIGIN/.."]
+            r = subprocess.run(cmd, capture_output=True, text=True)
+            if r.returncode != 0:
+                raise RuntimeError(f"driver build failed for {name}:\n{r.stderr}")
+        return exe
+    with cf.ThreadPoolExecutor(max_workers=len(DRIVERS)) as ex:
+        out = list(ex.map(one, DRIVERS))
+    return out
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv)
+    build_drivers(force="--force" in sys.argv)
     print(OUT)

@@ -277,6 +277,82 @@ int acu_proj_to_sino_dev(acu_ctx* c, int nproj, int ndet, int nrows, const float
     return ACU_OK;
 }
 
+int acu_normalize_stack_u16(acu_ctx* c, int mode, int nproj, long npix, const uint16_t* raw, int nflat,
+                            const uint16_t* flats, int ndark, const uint16_t* darks, float* out)
+{
+    CKRET(check_any(c));
+    if ((mode != 0 && mode != 1) || nproj < 0 || npix < 1 || !raw || nflat < 1 || !flats || !out ||
+        (mode == 1 && (ndark < 1 || !darks)))
+        return set_err(c, ACU_ERR_INVALID, "invalid normalisation arguments (mode %d)", mode);
+    if (nproj == 0) return ACU_OK;
+    DevBuf d_raw, d_fl, d_dk, d_ob, d_df, d_out;
+    cudaStream_t st = c->stream;
+    CK(c, d_fl.ensure(sizeof(uint16_t) * npix * nflat));
+    CK(c, d_ob.ensure(sizeof(float) * npix));
+    CK(c, d_df.ensure(sizeof(float) * npix));
+    CK(c, cudaMemcpyAsync(d_fl.p, flats, sizeof(uint16_t) * npix * nflat, cudaMemcpyHostToDevice, st));
+    launch_frame_average_u16(nflat, npix, d_fl.as<uint16_t>(), d_ob.as<float>(), st);
+    if (ndark > 0 && darks) {
+        CK(c, d_dk.ensure(sizeof(uint16_t) * npix * ndark));
+        CK(c, cudaMemcpyAsync(d_dk.p, darks, sizeof(uint16_t) * npix * ndark, cudaMemcpyHostToDevice, st));
+        launch_frame_average_u16(ndark, npix, d_dk.as<uint16_t>(), d_df.as<float>(), st);
+    } else {
+        CK(c, cudaMemsetAsync(d_df.p, 0, sizeof(float) * npix, st));
+    }
+    // stream the projections through in chunks of <= 1 GiB of output
+    const long chunk = std::max<long>(1, (long)((1u << 30) / (npix * sizeof(float))));
+    const long nc = std::min<long>(chunk, nproj);
+    CK(c, d_raw.ensure(sizeof(uint16_t) * npix * nc));
+    CK(c, d_out.ensure(sizeof(float) * npix * nc));
+    for (long p0 = 0; p0 < nproj; p0 += nc) {
+        const long n = std::min<long>(nc, nproj - p0);
+        CK(c, cudaMemcpyAsync(d_raw.p, raw + (size_t)p0 * npix, sizeof(uint16_t) * npix * n, cudaMemcpyHostToDevice,
+                              st));
+        launch_normalize_u16(mode, (int)n, npix, d_raw.as<uint16_t>(), d_ob.as<float>(), d_df.as<float>(),
+                             d_out.as<float>(), st);
+        CKLAUNCH(c);
+        CK(c, cudaMemcpyAsync(out + (size_t)p0 * npix, d_out.p, sizeof(float) * npix * n, cudaMemcpyDeviceToHost, st));
+    }
+    CK(c, cudaStreamSynchronize(st));
+    return ACU_OK;
+}
+
+int acu_proj_to_sino(acu_ctx* c, int nproj, int ndet, int nrows, const float* proj, const float* theta_deg,
+                     int reg_method, float* sino_out, float* theta_out, float* shift_out)
+{
+    CKRET(check_proj(c, ndet, nrows));
+    if (nproj < 1 || !proj || !theta_deg || !sino_out) return set_err(c, ACU_ERR_INVALID, "invalid arguments");
+    if (reg_method != 0 && reg_method != 1) return set_err(c, ACU_ERR_INVALID, "reg_method must be 0 or 1");
+    const size_t npix = (size_t)ndet * nrows;
+    const int add = ndet % 2 == 0 ? 1 : 0;
+    const size_t nsino = (size_t)nrows * nproj * (ndet + add);
+    DevBuf d_proj, d_p0, d_p180, d_sino;
+    CK(c, d_proj.ensure(sizeof(float) * npix * nproj));
+    CK(c, d_p0.ensure(sizeof(float) * npix));
+    CK(c, d_p180.ensure(sizeof(float) * npix));
+    CK(c, d_sino.ensure(sizeof(float) * nsino));
+    cudaStream_t st = c->stream;
+    CK(c, cudaMemcpyAsync(d_proj.p, proj, sizeof(float) * npix * nproj, cudaMemcpyHostToDevice, st));
+    CKRET(acu_pick_angle_dev(c, nproj, theta_deg, (long)npix, d_proj.as<float>(), 0.0f, d_p0.as<float>()));
+    CKRET(acu_pick_angle_dev(c, nproj, theta_deg, (long)npix, d_proj.as<float>(), 180.0f, d_p180.as<float>()));
+    float th = 0.0f, sh = 0.0f;
+    if (reg_method == 0) {
+        CKRET(acu_register_dev(c, ndet, nrows, d_p0.as<float>(), d_p180.as<float>(), &th, &sh, nullptr));
+    } else {
+        int kb;
+        double ks;
+        const int kmax = std::max(1, std::min(ndet / 4, 512));
+        CKRET(acu_xcorr_register_dev(c, ndet, nrows, d_p0.as<float>(), d_p180.as<float>(), kmax, nullptr, &kb, &ks));
+        sh = (float)(((double)add - ks) / (2.0 * ndet));
+    }
+    CKRET(acu_proj_to_sino_dev(c, nproj, ndet, nrows, d_proj.as<float>(), th, sh, d_sino.as<float>()));
+    CK(c, cudaMemcpyAsync(sino_out, d_sino.p, sizeof(float) * nsino, cudaMemcpyDeviceToHost, st));
+    CK(c, cudaStreamSynchronize(st));
+    if (theta_out) *theta_out = th;
+    if (shift_out) *shift_out = sh;
+    return ACU_OK;
+}
+
 int acu_proj_to_sino_u16(acu_ctx* c, int nproj, int ndet, int nrows, const uint16_t* raw, const float* theta_deg,
                          int nflat, const uint16_t* flats, int ndark, const uint16_t* darks, int norm_mode,
                          int reg_method, float* sino_out, float* theta_out, float* shift_out)

@@ -1,0 +1,62 @@
+// fbp_hpc: filtered backprojection of every slice -- the drop-in for
+// tomography/fbp_hpc.F90:156-425.  Reads input_parm.txt (only wpu matters:
+// the reference forces nsub = nsub_t = 1, :280-281), the 4-float fileinfo,
+// theta.dat and sinograms{k}.dat, and writes fbp{k}.dat.  The parameters are
+// not written back into the fileinfo (the reference's offsets 2-9 overwrite
+// clash with the 4-float layout the other programs read).  Slices are
+// reconstructed in batches of ACUMEN_BATCH (default 256) on the GPU.
+#include <chrono>
+#include <memory>
+
+#include "hpc_io.h"
+
+int main()
+{
+    try {
+        using namespace hpc;
+        const std::string dir = recon_dir();
+        const std::string parm = env("ROOT_CT_DIR") + "/" + env("EXP_CT_NAME") + "/input_parm.txt";
+        std::printf(" Updating from file: %s\n", parm.c_str());
+        const Params p = read_input_parm(parm);
+        const auto t0 = std::chrono::steady_clock::now();
+        const FileInfo fi = read_fileinfo(dir);
+        const int nimagef = fi.nimage, nfiles = fi.nfiles;
+        const std::vector<float> f_theta = read_theta(dir, nfiles);
+        const int jts = minloc_abs(f_theta, 0.0f), jte = minloc_abs(f_theta, 180.0f);
+        const int ntheta = jte - jts + 1;                                     // :324
+        const int add = nimagef % 2 == 0 ? 1 : 0;
+        const int nimage = nimagef + add;                                     // :329
+        std::vector<float> theta(f_theta.begin() + (jts - 1), f_theta.begin() + (jts - 1) + ntheta);
+        std::printf(" Reconstruction with Resolution: %d with %d projections\n", nimage, ntheta);
+        acu_ctx* ctx = nullptr;
+        check(acu_ctx_create(&ctx, nimage, ntheta, theta.data(), p.wpu), nullptr);
+        std::vector<std::unique_ptr<File>> fsino, frec;
+        for (int k = 1; k <= fi.n_files_sino; ++k) fsino.emplace_back(new File(fnum(dir + "sinograms", k), false));
+        for (int k = 1; k <= fi.n_files_rec; ++k) frec.emplace_back(new File(fnum(dir + "fbp", k), true));
+        const int batch = std::max(1, std::atoi((std::getenv("ACUMEN_BATCH") ? std::getenv("ACUMEN_BATCH") : "256")));
+        const size_t slab = (size_t)nimage * nfiles;
+        std::vector<float> sino(slab), f((size_t)batch * ntheta * nimage), img((size_t)batch * nimage * nimage);
+        for (int s0 = 1; s0 <= nimagef; s0 += batch) {
+            const int B = std::min(batch, nimagef - s0 + 1);
+            for (int b = 0; b < B; ++b) {
+                const Where w = locate(s0 + b, nimagef, fi.n_files_sino);      // :383-392
+                fsino[w.file - 1]->read(w.item * (long long)slab, sino.data(), slab);
+                std::memcpy(f.data() + (size_t)b * ntheta * nimage, sino.data() + (size_t)(jts - 1) * nimage,
+                            sizeof(float) * (size_t)ntheta * nimage);
+            }
+            check(acu_iradon(ctx, B, f.data(), img.data()), ctx);             // get_slice, :394
+            for (int b = 0; b < B; ++b) {
+                const Where w = locate(s0 + b, nimagef, fi.n_files_rec);      // :396-398
+                frec[w.file - 1]->write(w.item * (long long)nimage * nimage, img.data() + (size_t)b * nimage * nimage,
+                                        (size_t)nimage * nimage);
+            }
+        }
+        acu_ctx_destroy(ctx);
+        const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        std::printf(" Total Compute time: %g\n", secs);
+        return 0;
+    } catch (const std::exception& e) {
+        std::fprintf(stderr, "fbp_hpc: %s\n", e.what());
+        return 1;
+    }
+}

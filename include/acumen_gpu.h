@@ -193,6 +193,13 @@ int acu_resample_dev(acu_ctx *ctx, int ndet, int nrows, const float *d_src, floa
                      float *d_out);
 int acu_proj_to_sino_dev(acu_ctx *ctx, int nproj, int ndet, int nrows, const float *d_proj, float theta,
                          float shift, float *d_sino);
+/* Host-buffer forms used by the drivers: normalisation of a uint16 stack with
+ * its flat and dark stacks (fits_to_hpc.F90:183-248), and the chain from
+ * normalised float projections to sinograms (projections_to_sinogram_hpc.F90). */
+int acu_normalize_stack_u16(acu_ctx *ctx, int mode, int nproj, long npix, const uint16_t *raw, int nflat,
+                            const uint16_t *flats, int ndark, const uint16_t *darks, float *out);
+int acu_proj_to_sino(acu_ctx *ctx, int nproj, int ndet, int nrows, const float *proj, const float *theta_deg,
+                     int reg_method, float *sino_out, float *theta_out, float *shift_out);
 int acu_proj_to_sino_u16(acu_ctx *ctx, int nproj, int ndet, int nrows, const uint16_t *raw,
                          const float *theta_deg, int nflat, const uint16_t *flats, int ndark,
                          const uint16_t *darks, int norm_mode, int reg_method, float *sino_out,
