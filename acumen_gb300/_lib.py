@@ -84,6 +84,12 @@ SIGNATURES = {
     "acu_normalize_stack_u16": [P, I, I, L, P, I, P, I, P, P],
     "acu_proj_to_sino": [P, I, I, I, P, P, I, P, P, P],
     "acu_tv_loss_grad_dev": [P, I, P, P, P, F, F, P, P, P],
+    "acu_batch_create": [ctypes.POINTER(P), I, P, P, P, P],
+    "acu_batch_destroy": [P],
+    "acu_batch_set_stream": [P, P],
+    "acu_batch_tvopt": [P, P, I, I, I, F, F, P, P],
+    "acu_batch_op": [P, I, P, P],
+    "acu_batch_tuning": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
     "acu_tv_loss_grad_dev_f64": [P, I, P, P, P, D, D, P, P, P],
 }
 
@@ -104,6 +110,9 @@ def lib():
             fn.restype = I
         L.acu_last_error.argtypes = [P]
         L.acu_last_error.restype = ctypes.c_char_p
+        if hasattr(L, "acu_batch_last_error"):
+            L.acu_batch_last_error.argtypes = [P]
+            L.acu_batch_last_error.restype = ctypes.c_char_p
         _lib = L
     return _lib
 

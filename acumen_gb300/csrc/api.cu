@@ -159,8 +159,11 @@ int run_op_v(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
         if constexpr (V == 4 && sizeof(Real) == 4) {
             CK(c, c->pairP.ensure(sizeof(float) * 8 * nimg * G));
             CK(c, c->pairPT.ensure(sizeof(float) * 8 * nimg * G));
-            launch_radon_pairs(g, G, lin, c->pairP.template as<float>(), c->pairPT.template as<float>(), lout,
-                               c->stream);
+            if (c->opt_projector == 1)
+                launch_radon_quads(g, G, lin, c->pairPT.template as<float>(), lout, c->stream);
+            else
+                launch_radon_pairs(g, G, lin, c->pairP.template as<float>(), c->pairPT.template as<float>(), lout,
+                                   c->stream);
         } else {
             launch_radon<Real, V>(g, G, lin, lout, c->stream);
         }
@@ -231,9 +234,13 @@ struct TvRun {
     void iradon(const Real* sino, Real* img) { lanes_iradon<Real, V>(c, *g, G, sino, B(s->q), img); }
     void radon(const Real* img, Real* sino)
     {
-        if constexpr (V == 4 && sizeof(Real) == 4)
-            launch_radon_pairs(*g, G, img, c->pairP.template as<float>(), c->pairPT.template as<float>(), sino,
-                               c->stream);
+        if constexpr (V == 4 && sizeof(Real) == 4) {
+            if (c->opt_projector == 1)
+                launch_radon_quads(*g, G, img, c->pairPT.template as<float>(), sino, c->stream);
+            else
+                launch_radon_pairs(*g, G, img, c->pairP.template as<float>(), c->pairPT.template as<float>(), sino,
+                                   c->stream);
+        }
         else
             launch_radon<Real, V>(*g, G, img, sino, c->stream);
     }
@@ -683,6 +690,10 @@ int acu_set_option(acu_ctx* c, int option, int value)
         c->opt_print_every = value;
         return ACU_OK;
     case 6: c->opt_slice_base = value; return ACU_OK;
+    case 7:
+        if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 or 1");
+        c->opt_projector = value;
+        return ACU_OK;
     }
     return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
 }
@@ -697,6 +708,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case ACU_OPT_VERBOSE: *value = c->opt_verbose; return ACU_OK;
     case ACU_OPT_PRINT_EVERY: *value = c->opt_print_every; return ACU_OK;
     case 6: *value = c->opt_slice_base; return ACU_OK;
+    case 7: *value = c->opt_projector; return ACU_OK;
     }
     return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);
 }

@@ -33,6 +33,9 @@ void launch_radon(const DevGeom<Real>& g, int G, const Real* img, Real* sino, cu
 // work buffers of 2 * N * N * 4 floats per slice group each.
 void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float* P, float* PT, float* sino,
                         cudaStream_t st);
+// Same projector on the lane image and its transpose IT (N * N * 4 floats per
+// slice group), four 128-bit loads per sample.
+void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st);
 template <typename Real, int V>
 void launch_radon_adjoint(const DevGeom<Real>& g, int G, const Real* sino, Real* img, cudaStream_t st);
 template <typename Real, int V>

@@ -63,6 +63,8 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_GRAPH 3     /* 1: capture the Bregman outer iteration as a CUDA graph (default); 0: launch */
 #define ACU_OPT_VERBOSE 4   /* 1: print the reference's "Slice/Loop/delta" lines (tv_hpc.F90:350-352) */
 #define ACU_OPT_PRINT_EVERY 5 /* outer-loop period of those lines: 50 (tv_hpc) or 10 (tv_hpc_slice) */
+#define ACU_OPT_SLICE_BASE 6  /* slice number printed for the first slice of a call (default 1) */
+#define ACU_OPT_PROJECTOR 7   /* single-precision batched projector: 0 pair images (default), 1 image + transpose */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
 
@@ -204,6 +206,29 @@ int acu_proj_to_sino_u16(acu_ctx *ctx, int nproj, int ndet, int nrows, const uin
                          const float *theta_deg, int nflat, const uint16_t *flats, int ndark,
                          const uint16_t *darks, int norm_mode, int reg_method, float *sino_out,
                          float *theta_out, float *shift_out);
+
+/* ---- ragged batches: independent problems of different size ----------------
+ * nprob problems, problem i with grid side nimage[i], ntheta[i] angles (its
+ * angles at theta_concat[sum_{j<i} ntheta[j] ...]) and mask taper wpu[i];
+ * each problem is one slice.  acu_batch_tvopt solves all of them with
+ * tomography/tv_hpc.F90:162-363 (same ninner/nouter/ncg/lambda/mu), f holding
+ * the sinograms back to back (T_i*N_i floats each) and tv / fbp the images
+ * (N_i*N_i each), host buffers.  The projector and backprojection run as
+ * persistent kernels over (problem, angle, bin block) / (problem, pixel tile)
+ * work items, largest problem first, one launch per operator; their block
+ * shapes are chosen by timing candidates on the batch at first use
+ * (acu_batch_tuning reports the choice).  acu_batch_op runs one operator
+ * (op 0: radon, images -> sinograms; op 1: iradon, sinograms -> images).  */
+typedef struct acu_batch acu_batch;
+int acu_batch_create(acu_batch **batch, int nprob, const int *nimage, const int *ntheta, const float *theta_concat,
+                     const int *wpu);
+int acu_batch_destroy(acu_batch *batch);
+int acu_batch_set_stream(acu_batch *batch, void *cuda_stream);
+const char *acu_batch_last_error(const acu_batch *batch);
+int acu_batch_tvopt(acu_batch *batch, const float *f, int ninner, int nouter, int ncg, float lambda, float mu,
+                    float *tv_out, float *fbp_out);
+int acu_batch_op(acu_batch *batch, int op, const float *in, float *out);
+int acu_batch_tuning(const acu_batch *batch, int *radon_warps, int *bp_rows);
 
 /* ---- cross-correlation registration without device allocation --------------
  * No counterpart in the reference.  Same computation and results as

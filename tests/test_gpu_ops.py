@@ -145,3 +145,16 @@ def test_empty_batch_and_bad_shapes(case):
     assert out.shape == (0, case["N"], case["N"])
     with pytest.raises(ValueError):
         t.iradon(torch.zeros(case["T"] + 1, case["N"], device="cuda"))
+
+
+def test_projector_variants_agree(case, oracle):
+    """The two batched single-precision projectors (pair images, lane image +
+    transpose) compute the same sums up to summation order."""
+    t = Tomography(case["N"], case["th"], case["wpu"])
+    img = torch.from_numpy(case["img"][:5].astype(np.float32)).cuda()
+    t.set_option(7, 0)
+    a = t.radon(img)
+    t.set_option(7, 1)
+    b = t.radon(img)
+    assert rel(a, b) < 1e-6
+    assert rel(b, oracle.radon(case["img"][:5], case["th"], 64)) < 1e-6
