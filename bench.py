@@ -38,6 +38,10 @@ sys.path.insert(0, ROOT)
 METRIC = "TV slices/sec 2048²@1200 angles batched vs plain GPU at relL2≤1e-4; FBP GUPS"
 N_GRID, T_ANG, S_BATCH = 2049, 1200, 256
 NINNER, NCG, NOUTER, LAM, MU, WPU = 1, 10, 50, 0.05, 1.0, 100
+# DRAM bytes (read + write) of one k_radon_pairs launch per group of 4 slices at
+# 2049^2 x 1200 angles, from the ncu capture summarised in
+# profiles/k_radon_pairs_2049sq_1200ang_4slices.md (scaled by groups below)
+RADON_TRAFFIC_PER_GROUP = 37.14e9 + 43.6e6
 
 
 def parse():
@@ -182,6 +186,37 @@ def cpu_slices_per_s(N, T, threads=None):
 
 
 # ---------------------------------------------------------------------------
+def uneven_batch(nprob=64, seed=7):
+    import numpy as np
+    import torch
+    from acumen_gb300 import synthetic as syn
+    from acumen_gb300.batch import RaggedBatch
+    rng = np.random.default_rng(seed)
+    sides = rng.choice([256, 512, 1024, 1536, 2048], nprob)
+    Ns = [int(np.ceil(np.sqrt(2) * sd)) | 1 for sd in sides]
+    Ts = [int(rng.integers(180, 1501)) for _ in range(nprob)]
+    ths = [syn.angles(T) for T in Ts]
+    sinos = [syn.analytic_sinogram(syn.random_ellipses(500 + i, 0.5 * sd), N, th, device="cuda")
+             .float().cpu().numpy() for i, (sd, N, th) in enumerate(zip(sides, Ns, ths))]
+    b = RaggedBatch(Ns, ths, WPU)
+    b.tvopt(sinos, NINNER, 1, NCG, LAM, MU)             # tuning, graph capture
+    t0 = time.perf_counter()
+    b.tvopt(sinos, NINNER, 1, NCG, LAM, MU)
+    t1 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    b.tvopt(sinos, NINNER, 2, NCG, LAM, MU)
+    t2 = time.perf_counter() - t0
+    t_outer = max(t2 - t1, 1e-9)
+    t_job = t1 + (NOUTER - 1) * t_outer
+    w, r = b.tuning()
+    b.close()
+    return {"value": nprob / t_job, "unit": "problems/s", "problems": nprob, "outer_s": t_outer,
+            "grid_sides": sorted(set(Ns)), "angles": [min(Ts), max(Ts)],
+            "samples_per_outer": float(sum((NCG + 1) * T * N * N for N, T in zip(Ns, Ts))),
+            "tuned": {"radon_warps": w, "bp_rows": r},
+            "how": "host-buffer acu_batch_tvopt; t(nouter=1) + 49 x [t(nouter=2) - t(nouter=1)]"}
+
+
 def run_reference(args, rank, world):
     if rank != 0:
         return
@@ -302,12 +337,17 @@ def main():
         hbm, kind = measured_peaks()
         alg_bytes = 4.0 * (N * N + N * T) * S
         achieved = alg_bytes / t_radon / 1e9
-        line["roofline"] = {"bound": "hbm", "kernel": "k_radon (projector, tv_hpc.F90:137-156)",
+        groups = (S + 3) // 4
+        traffic = RADON_TRAFFIC_PER_GROUP * groups if (N, T) == (N_GRID, T_ANG) else None
+        line["roofline"] = {"bound": "hbm", "kernel": "k_radon_pairs (projector, tv_hpc.F90:137-156)",
                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                            "peak_kind": kind, "traffic": None,
+                            "peak_kind": kind, "traffic": traffic,
                             "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,
-                            "l1_level_GBps": 16.0 * N * N * T * S / t_radon / 1e9,
-                            "samples_per_s": N * N * T * S / t_radon}
+                            "note": "gather-bound on L1 wavefronts (ncu 91 %), not on HBM; traffic from one "
+                                    "4-slice ncu capture scaled by slice groups",
+                            "l1_level": {"achieved_GBps": 16.0 * N * N * T * S / t_radon / 1e9,
+                                         "bytes_per_sample_slice": 16,
+                                         "sample_slices_per_s": N * N * T * S / t_radon}}
         # end to end through the host-buffer C ABI: one outer iteration with copies
         fh = f.cpu().pin_memory()
         tvh = torch.empty(S, N, N, pin_memory=True)
@@ -343,6 +383,11 @@ def main():
         g1 = 725 * 725 * 720 / cuda_time(lambda: t1c.iradon(s1), 10) / 1e9
         gb = N * N * T * S / cuda_time(lambda: t.iradon(f), 2) / 1e9
         line["fbp_gups"] = {"config1_single_slice": g1, "batch_2049sq_1200_x256": gb}
+        # ragged batch (config 4 shape): 64 problems, grids {363,725,1449,2173,2897},
+        # 180-1500 angles; one outer iteration timed as tvopt(2) - tvopt(1)
+        del f
+        torch.cuda.empty_cache()
+        line["uneven_batch"] = uneven_batch()
         # CPU baseline (bounded sample, all host cores)
         v, ncores, desc = cpu_slices_per_s(N, T)
         line["cpu_baseline"] = {"value": v, "unit": "slices/s", "cores": ncores, "kind": "port", "sample": desc}
