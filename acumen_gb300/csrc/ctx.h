@@ -84,7 +84,7 @@ struct acu_ctx {
     int opt_verbose = 0;
     int opt_print_every = 50;
     int opt_slice_base = 1;
-    int opt_projector = 0;   // single-precision projector: 0 pair images, 1 lane image + transpose
+    int opt_projector = 1;   // single-precision projector: 0 pair images, 1 lane image + transpose
     std::string err;
     acu::GeomSet<float> g32;
     acu::GeomSet<double> g64;

@@ -38,10 +38,11 @@ sys.path.insert(0, ROOT)
 METRIC = "TV slices/sec 2048²@1200 angles batched vs plain GPU at relL2≤1e-4; FBP GUPS"
 N_GRID, T_ANG, S_BATCH = 2049, 1200, 256
 NINNER, NCG, NOUTER, LAM, MU, WPU = 1, 10, 50, 0.05, 1.0, 100
-# DRAM bytes (read + write) of one k_radon_pairs launch per group of 4 slices at
-# 2049^2 x 1200 angles, from the ncu capture summarised in
-# profiles/k_radon_pairs_2049sq_1200ang_4slices.md (scaled by groups below)
-RADON_TRAFFIC_PER_GROUP = 37.14e9 + 43.6e6
+# DRAM bytes (read + write) of one projector launch (k_radon_quads plus its
+# k_make_transpose) per group of 4 slices at 2049^2 x 1200 angles, from the ncu
+# capture summarised in profiles/k_radon_quads_2049sq_1200ang_4slices.md
+# (scaled by groups below)
+RADON_TRAFFIC_PER_GROUP = (300.71e6 + 36.85e6) + (67.21e6 + 17.78e6)
 
 
 def parse():
@@ -148,6 +149,24 @@ def cuda_time(fn, reps, stream=None):
     e1.record()
     torch.cuda.synchronize()
     return e0.elapsed_time(e1) / 1000.0 / reps
+
+
+# ---------------------------------------------------------------------------
+def max_over_ranks(values, world, device):
+    """Timing of the slowest rank (the ranks share no data: each solves its own
+    batch, so the only collective is this reduction of step times)."""
+    if world <= 1:
+        return list(values)
+    import torch
+    import torch.distributed as dist
+    tt = torch.tensor(list(values), device=device, dtype=torch.float64)
+    dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+    return tt.tolist()
+
+
+def job_value(world, slices_per_rank, t_warm, t_step):
+    """Whole-job slices/s of the full nouter-iteration reconstruction, all ranks."""
+    return world * slices_per_rank / (t_warm + NOUTER * t_step)
 
 
 # ---------------------------------------------------------------------------
@@ -305,12 +324,8 @@ def main():
     torch.cuda.synchronize()
     clocks = sampler.stop()
     t_step = e0.elapsed_time(e1) / 1000.0 / args.steps
-    if world > 1:
-        tt = torch.tensor([t_step, t_warm], device="cuda", dtype=torch.float64)
-        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        t_step, t_warm = tt.tolist()
-    t_job = t_warm + NOUTER * t_step
-    value = world * S / t_job
+    t_step, t_warm = max_over_ranks([t_step, t_warm], world, "cuda")
+    value = job_value(world, S, t_warm, t_step)
     # kernels of one outer iteration (the captured graph): projector launches,
     # filter + backprojection per iradon, and the element-wise / finaliser kernels
     n_radon = NINNER * NCG + (NINNER - 1) + 1
@@ -339,11 +354,11 @@ def main():
         achieved = alg_bytes / t_radon / 1e9
         groups = (S + 3) // 4
         traffic = RADON_TRAFFIC_PER_GROUP * groups if (N, T) == (N_GRID, T_ANG) else None
-        line["roofline"] = {"bound": "hbm", "kernel": "k_radon_pairs (projector, tv_hpc.F90:137-156)",
+        line["roofline"] = {"bound": "hbm", "kernel": "k_radon_quads (projector, tv_hpc.F90:137-156)",
                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                             "peak_kind": kind, "traffic": traffic,
                             "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,
-                            "note": "gather-bound on L1 wavefronts (ncu 91 %), not on HBM; traffic from one "
+                            "note": "gather-bound on L1 wavefronts (ncu 97 %), not on HBM; traffic from one "
                                     "4-slice ncu capture scaled by slice groups",
                             "l1_level": {"achieved_GBps": 16.0 * N * N * T * S / t_radon / 1e9,
                                          "bytes_per_sample_slice": 16,

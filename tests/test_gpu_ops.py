@@ -148,13 +148,17 @@ def test_empty_batch_and_bad_shapes(case):
 
 
 def test_projector_variants_agree(case, oracle):
-    """The two batched single-precision projectors (pair images, lane image +
-    transpose) compute the same sums up to summation order."""
+    """The two batched single-precision projector variants (pair images; lane
+    image + transpose) compute the same sums up to summation order, also on
+    random images that reach the border."""
     t = Tomography(case["N"], case["th"], case["wpu"])
-    img = torch.from_numpy(case["img"][:5].astype(np.float32)).cuda()
-    t.set_option(7, 0)
-    a = t.radon(img)
-    t.set_option(7, 1)
-    b = t.radon(img)
-    assert rel(a, b) < 1e-6
-    assert rel(b, oracle.radon(case["img"][:5], case["th"], 64)) < 1e-6
+    rng = np.random.default_rng(5)
+    for x in (case["img"][:5].astype(np.float32), rng.standard_normal((5, case["N"], case["N"])).astype(np.float32)):
+        img = torch.from_numpy(x).cuda()
+        outs = []
+        for v in (0, 1):
+            t.set_option(7, v)
+            outs.append(t.radon(img))
+        ref = oracle.radon(x, case["th"], 32)
+        for o in outs:
+            assert rel(o, ref) < 1e-6
