@@ -164,6 +164,9 @@ int run_op_v(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
             else
                 launch_radon_pairs(g, G, lin, c->pairP.template as<float>(), c->pairPT.template as<float>(), lout,
                                    c->stream);
+        } else if constexpr (V == 1 && sizeof(Real) == 4) {
+            CK(c, c->pairPT.ensure(sizeof(float) * nimg * G));
+            launch_radon_v1_fast(g, G, lin, c->pairPT.template as<float>(), lout, c->stream);
         } else {
             launch_radon<Real, V>(g, G, lin, lout, c->stream);
         }
@@ -234,7 +237,9 @@ struct TvRun {
     void iradon(const Real* sino, Real* img) { lanes_iradon<Real, V>(c, *g, G, sino, B(s->q), img); }
     void radon(const Real* img, Real* sino)
     {
-        if constexpr (V == 4 && sizeof(Real) == 4) {
+        if constexpr (V == 1 && sizeof(Real) == 4) {
+            launch_radon_v1_fast(*g, G, img, c->pairPT.template as<float>(), sino, c->stream);
+        } else if constexpr (V == 4 && sizeof(Real) == 4) {
             if (c->opt_projector == 1)
                 launch_radon_quads(*g, G, img, c->pairPT.template as<float>(), sino, c->stream);
             else
@@ -309,6 +314,8 @@ int tv_begin_v(acu_ctx* c, int S, const Real* d_f, int ninner, int ncg, double l
     if constexpr (V == 4 && sizeof(Real) == 4) {
         CK(c, c->pairP.ensure(sizeof(float) * 2 * nimg));
         CK(c, c->pairPT.ensure(sizeof(float) * 2 * nimg));
+    } else if constexpr (sizeof(Real) == 4) {
+        CK(c, c->pairPT.ensure(sizeof(float) * nimg));
     }
     const int Sp = G * V;
     s.nblk = (int)std::min<size_t>(((size_t)N * N + 255) / 256, 512);

@@ -23,6 +23,39 @@
 
 namespace acu {
 
+// One staggered ray of the single-slice projector (as radon_stag_ray<1> in
+// kernels_radon.cu).
+__device__ __forceinline__ void radon_stag_ray_v1(const float* __restrict__ I, const float* __restrict__ IT, int N,
+                                                  float s, float c, float mid, int jy, int lane, bool transposed,
+                                                  float (&acc)[1])
+{
+    const float ratio = transposed ? -s / c : c / s;
+    const int kb = __float2int_rn((float)lane * ratio);
+    const int kend = __float2int_rn(31.f * ratio);
+    const int kmin = min(0, kend), kmax = max(0, kend);
+    const float dyv = (float)jy - mid;
+    const float sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+    const float* base = transposed ? IT : I;
+    for (int i = 1 + kmin; i <= N + kmax; ++i) {
+        const int jx = i - kb;
+        if (jx < 1 || jx > N || jy > N) continue;
+        const float dxv = (float)jx - mid;
+        const float xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
+        const float yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
+        const float x1f = floorf(xr), y1f = floorf(yr);
+        const int x1 = (int)x1f, y1 = (int)y1f;
+        if (min(x1, y1) > 1 && max(x1, y1) < N) {
+            const float wxl = add_rn(x1f, 1.f) - xr, wxh = xr - x1f;
+            const float wyl = add_rn(y1f, 1.f) - yr, wyh = yr - y1f;
+            const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
+            const int r0 = transposed ? x1 : y1, c0 = transposed ? y1 : x1;
+            const float* q = base + (size_t)(r0 - 1) * N + (c0 - 1);
+            const float wb = transposed ? w12 : w21, wc = transposed ? w21 : w12;
+            acc[0] = fmaf(__ldg(q + N + 1), w22, fmaf(__ldg(q + N), wc, fmaf(__ldg(q + 1), wb, fmaf(__ldg(q), w11, acc[0]))));
+        }
+    }
+}
+
 // problem of item `it` in a list whose per-problem first items are field F
 template <long long ProbDesc::*F>
 __device__ __forceinline__ int find_prob(const ProbDesc* __restrict__ pd, int nprob, long long it)
@@ -39,9 +72,12 @@ __device__ __forceinline__ int find_prob(const ProbDesc* __restrict__ pd, int np
 }
 
 // ---- projector: one warp item = 32 rays of one angle of one problem --------
+// Staggered rays through the image or its transpose (whichever the warp's
+// rays spread along), as the uniform projector.
 __global__ void __launch_bounds__(512) k_batch_radon(const ProbDesc* __restrict__ pd, int nprob,
-                                                     const float* __restrict__ img, float* __restrict__ sino,
-                                                     const float* __restrict__ sc, long long total, int* counter)
+                                                     const float* __restrict__ img, const float* __restrict__ IT,
+                                                     float* __restrict__ sino, const float* __restrict__ sc,
+                                                     long long total, int* counter)
 {
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -55,28 +91,34 @@ __global__ void __launch_bounds__(512) k_batch_radon(const ProbDesc* __restrict_
         const int t = local / d.nbx, b = local % d.nbx;
         const int jy = b * 32 + lane + 1;
         const int N = d.N;
-        if (jy > N) continue;
         const float s = sc[d.sc + 2 * t], c = sc[d.sc + 2 * t + 1];
-        const float mid = d.mid;
-        const float dyv = (float)jy - mid;
-        const float sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
-        const float* u = img + d.img;
-        float acc = 0.f;
-        for (int jx = 1; jx <= N; ++jx) {
-            const float dxv = (float)jx - mid;
-            const float xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
-            const float yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
-            const float x1f = floorf(xr), y1f = floorf(yr);
-            const int x1 = (int)x1f, y1 = (int)y1f;
-            if (min(x1, y1) > 1 && max(x1, y1) < N) {
-                const float wxl = add_rn(x1f, 1.f) - xr, wxh = xr - x1f;
-                const float wyl = add_rn(y1f, 1.f) - yr, wyh = yr - y1f;
-                const float* q = u + (size_t)(y1 - 1) * N + (x1 - 1);
-                acc = fmaf(__ldg(q + N + 1), wxh * wyh,
-                           fmaf(__ldg(q + N), wxl * wyh, fmaf(__ldg(q + 1), wxh * wyl, fmaf(__ldg(q), wxl * wyl, acc))));
-            }
-        }
-        sino[d.sino + (size_t)t * N + (jy - 1)] = acc / (float)N;
+        float acc[1] = {0.f};
+        radon_stag_ray_v1(img + d.img, IT + d.img, N, s, c, d.mid, jy, lane, fabsf(c) > fabsf(s), acc);
+        if (jy <= N) sino[d.sino + (size_t)t * N + (jy - 1)] = acc[0] / (float)N;
+    }
+}
+
+// transposed copies of every problem's image, one block per 32 x 32 tile
+__global__ void __launch_bounds__(256) k_batch_transpose(const ProbDesc* __restrict__ pd, int nprob,
+                                                         const float* __restrict__ img, float* __restrict__ IT)
+{
+    __shared__ float tile[32][33];
+    const long long it = blockIdx.x;
+    const int p = find_prob<&ProbDesc::it_tr>(pd, nprob, it);
+    const ProbDesc d = pd[p];
+    const int N = d.N, nt = (N + 31) / 32;
+    const int local = (int)(it - d.it_tr);
+    const int x0 = (local % nt) * 32, y0 = (local / nt) * 32;
+    const float* src = img + d.img;
+    float* dst = IT + d.img;
+    for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+        const int ty = i / 32, tx = i % 32;
+        if (x0 + tx < N && y0 + ty < N) tile[ty][tx] = src[(size_t)(y0 + ty) * N + x0 + tx];
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+        const int ty = i / 32, tx = i % 32;
+        if (x0 + ty < N && y0 + tx < N) dst[(size_t)(x0 + ty) * N + y0 + tx] = tile[tx][ty];
     }
 }
 
@@ -391,10 +433,11 @@ static int sm_count()
 
 void batch_radon(const BatchDev& b, const float* img, float* sino, int slot, cudaStream_t st)
 {
+    k_batch_transpose<<<(unsigned)b.n_tr, 256, 0, st>>>(b.pd, b.nprob, img, b.IT);
     cudaMemsetAsync(b.counter + slot, 0, sizeof(int), st);
     const int threads = 32 * b.radon_warps;
     const int blocks = sm_count() * (2048 / threads);
-    k_batch_radon<<<blocks, threads, 0, st>>>(b.pd, b.nprob, img, sino, b.sc_fp, b.n_radon, b.counter + slot);
+    k_batch_radon<<<blocks, threads, 0, st>>>(b.pd, b.nprob, img, b.IT, sino, b.sc_fp, b.n_radon, b.counter + slot);
 }
 void batch_backproject(const BatchDev& b, const float* q, float* img, int slot, cudaStream_t st)
 {
@@ -467,7 +510,7 @@ struct acu_batch {
     std::vector<int> order;           // execution order (largest work first) -> caller index
     BatchDev dev;
     DevBuf d_pd, d_sc_bp, d_sc_fp, d_cm, d_fh, d_tw, d_counter;
-    DevBuf f, fk, ruk, rp, q, uk, dx, dy, bx, by, rhs, r, p, Ap, tmp, part, rsold, alpha, beta;
+    DevBuf f, fk, ruk, rp, q, uk, dx, dy, bx, by, rhs, r, p, Ap, tmp, part, rsold, alpha, beta, it_img;
     DevBuf io_in, io_out;
     cudaGraphExec_t graph = nullptr;
     std::string graph_key;
@@ -608,7 +651,7 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
         return berr(b.get(), ACU_ERR_UNSUPPORTED, "a problem needs an FFT longer than 8192 (grid side > 4097)");
     b->desc.resize(nprob);
     std::vector<float> sc_bp, sc_fp, cm, fh;
-    long long img = 0, sino = 0, ir = 0, ib = 0, iff = 0, ie = 0;
+    long long img = 0, sino = 0, ir = 0, ib = 0, iff = 0, ie = 0, itr = 0;
     std::vector<ProbDesc> exec_desc;
     for (int k = 0; k < nprob; ++k) {
         const int i = b->order[k];
@@ -639,6 +682,8 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
         ib += (long long)((d.N + 31) / 32) * ((d.N + 3) / 4);   // rows of the smallest tile height
         iff += (d.T + 1) / 2;
         ie += ((long long)d.N * d.N + EWB - 1) / EWB;
+        d.it_tr = itr;
+        itr += (long long)((d.N + 31) / 32) * ((d.N + 31) / 32);
         b->desc[i] = d;
         exec_desc.push_back(d);
     }
@@ -675,6 +720,7 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
     d.n_bp = ib;
     d.n_fft = iff;
     d.n_ew = ie;
+    d.n_tr = itr;
     d.img_total = img;
     d.sino_total = sino;
     d.counter = b->d_counter.as<int>();
@@ -727,8 +773,9 @@ int ensure_state(acu_batch* b)
     acu_ctx* c = b->ctx;
     const size_t ni = sizeof(float) * (size_t)b->dev.img_total, ns = sizeof(float) * (size_t)b->dev.sino_total;
     for (DevBuf* x : {&b->f, &b->fk, &b->ruk, &b->rp, &b->q}) CK(c, x->ensure(ns));
-    for (DevBuf* x : {&b->uk, &b->dx, &b->dy, &b->bx, &b->by, &b->rhs, &b->r, &b->p, &b->Ap, &b->tmp})
+    for (DevBuf* x : {&b->uk, &b->dx, &b->dy, &b->bx, &b->by, &b->rhs, &b->r, &b->p, &b->Ap, &b->tmp, &b->it_img})
         CK(c, x->ensure(ni));
+    b->dev.IT = b->it_img.as<float>();
     CK(c, b->part.ensure(sizeof(double) * (size_t)b->dev.n_ew));
     for (DevBuf* x : {&b->rsold, &b->alpha, &b->beta}) CK(c, x->ensure(sizeof(double) * b->nprob));
     return ACU_OK;

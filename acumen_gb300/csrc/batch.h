@@ -22,6 +22,7 @@ struct ProbDesc {
     long long it_bp;        // first backprojection item: ceil(N/32) * ceil(N/8)
     long long it_fft;       // first filter item: ceil(T/2)
     long long it_ew;        // first element-wise block: ceil(N*N / 1024)
+    long long it_tr;        // first transpose tile: ceil(N/32)^2
 };
 
 struct BatchDev {
@@ -33,7 +34,8 @@ struct BatchDev {
     const float* fft_h = nullptr;
     const float2* tw = nullptr;   // twiddles of the largest L (Lmax entries)
     int Lmax = 0;
-    long long n_radon = 0, n_bp = 0, n_fft = 0, n_ew = 0;   // item totals
+    long long n_radon = 0, n_bp = 0, n_fft = 0, n_ew = 0, n_tr = 0;   // item totals
+    float* IT = nullptr;          // work buffer: transposed images (img_total floats)
     long long img_total = 0, sino_total = 0;
     int* counter = nullptr;       // work counters (one per persistent kernel)
     int radon_warps = 4;          // autotuned: warps per projector block

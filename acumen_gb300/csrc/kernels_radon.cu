@@ -274,24 +274,20 @@ __global__ void __launch_bounds__(256) k_make_transpose(const float* __restrict_
     }
 }
 
-__global__ void __launch_bounds__(128) k_radon_quads(const float* __restrict__ I, const float* __restrict__ IT,
-                                                     const float* __restrict__ sc, const int* __restrict__ order,
-                                                     float* __restrict__ sino, int N, int T, float mid)
+// One ray of the staggered projector, V slices per pixel (V = 1 or 4), read
+// from the copy selected by `transposed` (row = y1 in I, row = x1 in IT).
+template <int V>
+__device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, const float* __restrict__ IT, int N,
+                                               float s, float c, float mid, int jy, int lane, bool transposed,
+                                               float (&acc)[V])
 {
-    const int lane = threadIdx.x & 31;
-    const int jy = blockIdx.x * 128 + threadIdx.y * 32 + lane + 1;
-    const int t = order[blockIdx.y];
-    const int g = blockIdx.z;
-    const float s = sc[2 * t], c = sc[2 * t + 1];
-    const bool transposed = fabsf(c) > fabsf(s);
     const float ratio = transposed ? -s / c : c / s;
     const int kb = __float2int_rn((float)lane * ratio);
     const int kend = __float2int_rn(31.f * ratio);
     const int kmin = min(0, kend), kmax = max(0, kend);
     const float dyv = (float)jy - mid;
     const float sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
-    const float* base = (transposed ? IT : I) + (size_t)g * N * N * 4;
-    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    const float* base = transposed ? IT : I;
     for (int i = 1 + kmin; i <= N + kmax; ++i) {
         const int jx = i - kb;
         if (jx < 1 || jx > N || jy > N) continue;
@@ -305,22 +301,69 @@ __global__ void __launch_bounds__(128) k_radon_quads(const float* __restrict__ I
             const float wyl = add_rn(y1f, 1.f) - yr, wyh = yr - y1f;
             const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
             const int r0 = transposed ? x1 : y1, c0 = transposed ? y1 : x1;
-            const float* p = base + ((size_t)(r0 - 1) * N + (c0 - 1)) * 4;
-            const float4 a = __ldg(reinterpret_cast<const float4*>(p));
-            const float4 b = __ldg(reinterpret_cast<const float4*>(p + 4));
-            const float4 cc = __ldg(reinterpret_cast<const float4*>(p + (size_t)N * 4));
-            const float4 d = __ldg(reinterpret_cast<const float4*>(p + (size_t)N * 4 + 4));
+            const float* p = base + ((size_t)(r0 - 1) * N + (c0 - 1)) * V;
+            // a = (r0, c0); b = (r0, c0+1); cc = (r0+1, c0); d = (r0+1, c0+1)
+            const Lanes<float, V> a = ld_lanes<float, V>(p);
+            const Lanes<float, V> b = ld_lanes<float, V>(p + V);
+            const Lanes<float, V> cc = ld_lanes<float, V>(p + (size_t)N * V);
+            const Lanes<float, V> d = ld_lanes<float, V>(p + (size_t)N * V + V);
             const float wb = transposed ? w12 : w21, wc = transposed ? w21 : w12;
-            acc[0] = fmaf(d.x, w22, fmaf(cc.x, wc, fmaf(b.x, wb, fmaf(a.x, w11, acc[0]))));
-            acc[1] = fmaf(d.y, w22, fmaf(cc.y, wc, fmaf(b.y, wb, fmaf(a.y, w11, acc[1]))));
-            acc[2] = fmaf(d.z, w22, fmaf(cc.z, wc, fmaf(b.z, wb, fmaf(a.z, w11, acc[2]))));
-            acc[3] = fmaf(d.w, w22, fmaf(cc.w, wc, fmaf(b.w, wb, fmaf(a.w, w11, acc[3]))));
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                acc[v] = fmaf(d.v[v], w22, fmaf(cc.v[v], wc, fmaf(b.v[v], wb, fmaf(a.v[v], w11, acc[v]))));
         }
     }
+}
+
+template <int V>
+__global__ void __launch_bounds__(128) k_radon_stag(const float* __restrict__ I, const float* __restrict__ IT,
+                                                    const float* __restrict__ sc, const int* __restrict__ order,
+                                                    float* __restrict__ sino, int N, int T, float mid)
+{
+    const int lane = threadIdx.x & 31;
+    const int jy = blockIdx.x * 128 + threadIdx.y * 32 + lane + 1;
+    const int t = order[blockIdx.y];
+    const int g = blockIdx.z;
+    const float s = sc[2 * t], c = sc[2 * t + 1];
+    float acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = 0.f;
+    radon_stag_ray<V>(I + (size_t)g * N * N * V, IT + (size_t)g * N * N * V, N, s, c, mid, jy, lane,
+                      fabsf(c) > fabsf(s), acc);
     if (jy <= N) {
-        float4 o = make_float4(acc[0] / (float)N, acc[1] / (float)N, acc[2] / (float)N, acc[3] / (float)N);
-        *reinterpret_cast<float4*>(sino + (((size_t)g * T + t) * N + (jy - 1)) * 4) = o;
+        Lanes<float, V> o;
+#pragma unroll
+        for (int v = 0; v < V; ++v) o.v[v] = acc[v] / (float)N;
+        st_lanes<float, V>(sino + (((size_t)g * T + t) * N + (jy - 1)) * V, o);
     }
+}
+
+// transpose of a lane image, 32 x 32 tiles through shared memory (V = 1 or 4)
+template <int V>
+__global__ void __launch_bounds__(256) k_transpose_lanes(const float* __restrict__ img, float* __restrict__ IT, int N)
+{
+    __shared__ Lanes<float, V> tile[32][33];
+    const int g = blockIdx.z;
+    const int x0 = blockIdx.x * 32, y0 = blockIdx.y * 32;
+    const float* src = img + (size_t)g * N * N * V;
+    float* dst = IT + (size_t)g * N * N * V;
+    for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+        const int ty = i / 32, tx = i % 32;
+        if (x0 + tx < N && y0 + ty < N) tile[ty][tx] = ld_lanes_rw<float, V>(src + ((size_t)(y0 + ty) * N + x0 + tx) * V);
+    }
+    __syncthreads();
+    for (int i = threadIdx.x; i < 32 * 32; i += blockDim.x) {
+        const int ty = i / 32, tx = i % 32;
+        if (x0 + ty < N && y0 + tx < N) st_lanes<float, V>(dst + ((size_t)(x0 + ty) * N + y0 + tx) * V, tile[tx][ty]);
+    }
+}
+
+void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, float* IT, float* sino, cudaStream_t st)
+{
+    dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, S);
+    k_transpose_lanes<1><<<gp, bp, 0, st>>>(img, IT, g.N);
+    dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, S);
+    k_radon_stag<1><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.fp_order, sino, g.N, g.T, g.mid);
 }
 
 void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st)
@@ -328,7 +371,7 @@ void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float*
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
     k_make_transpose<<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, G);
-    k_radon_quads<<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    k_radon_stag<4><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.fp_order, sino, g.N, g.T, g.mid);
 }
 
 void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float* P, float* PT, float* sino,

@@ -205,6 +205,79 @@ def cpu_slices_per_s(N, T, threads=None):
 
 
 # ---------------------------------------------------------------------------
+def accuracy():
+    """Errors against FP64 at the configurations' full sizes.  The FP64 reference
+    here is the library's double-precision solver, itself checked against the
+    FP64 CPU oracle to 1e-9 at test sizes (tests/test_gpu_tv.py)."""
+    import numpy as np
+    import torch
+    from acumen_gb300 import synthetic as syn
+    from acumen_gb300.tomography import Tomography
+
+    def rel(a, b, m=None):
+        a, b = a.double(), b.double()
+        if m is not None:
+            a, b = a[..., m], b[..., m]
+        return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+
+    out = {}
+    # config 2: single-slice TV, 1449 grid (1448 bins made odd), 900 angles, I0 = 5e3, 50 x 10
+    N, T = 1449, 900
+    th = syn.angles(T)
+    f = syn.normalised_sinogram(syn.random_ellipses(2, 0.35 * N), N, th, I0=5e3, seed=2, device="cuda")[None]
+    t = Tomography(N, th, WPU)
+    tv32, fbp32 = t.tvopt(f.float(), NINNER, NOUTER, NCG, LAM, MU)
+    tv64, fbp64 = t.tvopt(f.double(), NINNER, NOUTER, NCG, LAM, MU)
+    tvp, _ = t.tvopt(f.float(), NINNER, NOUTER, NCG, LAM, MU, plain=True)
+    mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0]   # cmask support
+    out["config2_tv"] = {"rel_l2_disc_vs_fp64": rel(tv32, tv64, mask), "rel_l2_full_vs_fp64": rel(tv32, tv64),
+                         "plain_rel_l2_disc_vs_fp64": rel(tvp, tv64, mask),
+                         "fbp_rel_l2_vs_fp64": rel(fbp32, fbp64), "grid": N, "angles": T,
+                         "iterations": f"{NOUTER} x {NCG}"}
+    t.close()
+    # config 1: FBP of 725^2 at 720 angles
+    N, T = 725, 720
+    th, ell, counts, flat, dark = syn.config1_sinogram(seed=1, device="cuda")
+    p = (-torch.log(torch.clamp(counts - dark, min=1e-16) / max(flat - dark, 1.0))).float()[None]
+    t = Tomography(N, th, WPU)
+    out["config1_fbp"] = {"rel_l2_vs_fp64": rel(t.iradon(p), t.iradon(p.double())), "grid": N, "angles": T}
+    t.close()
+    return out
+
+
+def pipeline(nproj=1200, ndet=2048, nrows=256, seed=3):
+    """Config 3's preprocessing: raw uint16 projections with flat/dark stacks and
+    a random rotation-axis offset in [-8, 8] px -> averages, normalisation,
+    0/180 picks, registration, median, resample, transpose to 256 sinograms,
+    through the host-buffer C ABI (acu_proj_to_sino_u16)."""
+    import numpy as np
+    import torch
+    from acumen_gb300 import synthetic as syn
+    from acumen_gb300.preprocess import Preprocessor
+    rng = np.random.default_rng(seed)
+    offset = float(rng.uniform(-8, 8))
+    th, raw, flats, darks = syn.projection_stack(nproj, ndet, nrows, offset, seed, device="cuda")
+    u16 = lambda x: x.to(torch.int32).cpu().numpy().astype(np.uint16)
+    raw, flats, darks = u16(raw), u16(flats), u16(darks)
+    pp = Preprocessor()
+    out = {}
+    for reg in (0, 1):
+        pp.proj_to_sino_u16(raw[:8], th[:8], flats, darks, norm_mode=1, reg_method=reg)   # warm
+        t0 = time.perf_counter()
+        sino, theta_b, shift_b = pp.proj_to_sino_u16(raw, th, flats, darks, norm_mode=1, reg_method=reg)
+        dt = time.perf_counter() - t0
+        add = 1 if ndet % 2 == 0 else 0
+        axis_true = (ndet + add + 1) // 2 + offset
+        axis_found = (ndet + add + 1) / 2 - shift_b * ndet
+        out["pattern_search" if reg == 0 else "xcorr"] = {
+            "seconds": dt, "projections_per_s": nproj / dt, "theta_rad": theta_b,
+            "axis_error_px": axis_found - axis_true}
+    pp.close()
+    out.update({"offset_px": offset, "shape": [nproj, nrows, ndet], "input": "uint16 + 10 flat + 10 dark",
+                "how": "host buffers in and out (1.26 GB in, 2.5 GB of sinograms out)"})
+    return out
+
+
 def uneven_batch(nprob=64, seed=7):
     import numpy as np
     import torch
@@ -326,12 +399,13 @@ def main():
     t_step = e0.elapsed_time(e1) / 1000.0 / args.steps
     t_step, t_warm = max_over_ranks([t_step, t_warm], world, "cuda")
     value = job_value(world, S, t_warm, t_step)
-    # kernels of one outer iteration (the captured graph): projector launches,
-    # filter + backprojection per iradon, and the element-wise / finaliser kernels
+    # kernels of one outer iteration (the captured graph): transpose + projector
+    # per radon, filter + backprojection per iradon, and the element-wise /
+    # finaliser kernels (101 for ninner=1, ncg=10; the ncu launch list agrees)
     n_radon = NINNER * NCG + (NINNER - 1) + 1
     n_iradon = NINNER * (2 + NCG)
     n_ew = NINNER * (4 + 5 * NCG) + 1
-    kernel_launches = n_radon + 2 * n_iradon + n_ew
+    kernel_launches = 2 * n_radon + 2 * n_iradon + n_ew
 
     line = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True, "scaling": "weak",
@@ -403,6 +477,8 @@ def main():
         del f
         torch.cuda.empty_cache()
         line["uneven_batch"] = uneven_batch()
+        line["pipeline"] = pipeline()
+        line["accuracy"] = accuracy()
         # CPU baseline (bounded sample, all host cores)
         v, ncores, desc = cpu_slices_per_s(N, T)
         line["cpu_baseline"] = {"value": v, "unit": "slices/s", "cores": ncores, "kind": "port", "sample": desc}

@@ -109,3 +109,17 @@ def test_verbose_reports_err_diff(prob, capfd):
     assert out.count("Slice:") == 4 and "delta:" in out
     d = t.last_delta(2)
     assert np.all(d > 0)
+
+
+def test_fp32_tracks_fp64_at_larger_size(built_lib):
+    """725 grid, 360 angles, 20 x 10 iterations: the single-precision batched
+    solver against the library's double-precision solver (itself pinned to the
+    FP64 oracle above), inside the reconstruction disc."""
+    N, T, wpu = 725, 360, 50
+    th = syn.angles(T)
+    f = syn.normalised_sinogram(syn.random_ellipses(8, 0.35 * N), N, th, I0=5e3, seed=8, device="cuda")[None]
+    t = Tomography(N, th, wpu)
+    tv32, _ = t.tvopt(f.float(), 1, 20, 10, 0.05, 1.0)
+    tv64, _ = t.tvopt(f.double(), 1, 20, 10, 0.05, 1.0)
+    mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0].cpu().numpy()
+    assert rel(tv32, tv64, mask) < TV_TOL
