@@ -60,6 +60,8 @@ SIGNATURES = {
     "acu_iradon_dev_f64": [P, I, P, P],
     "acu_radon_dev_f64": [P, I, P, P],
     "acu_radon_adjoint_dev_f64": [P, I, P, P],
+    "acu_filter_dev_f64": [P, I, P, P],
+    "acu_backproject_dev_f64": [P, I, P, P],
     "acu_tvopt": [P, I, P, I, I, I, F, F, P, P],
     "acu_tvopt_dev": [P, I, P, I, I, I, F, F, P, P],
     "acu_tvopt_plain": [P, I, P, I, I, I, F, F, P, P],

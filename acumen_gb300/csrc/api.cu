@@ -355,8 +355,8 @@ int tv_iterate_v(acu_ctx* c, int nouter)
     const bool use_graph = c->opt_graph != 0 && !run.verbose;
     if (use_graph) {
         char key[256];
-        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
-                 s.ncg, s.lambda, s.mu, c->opt_filter, s.uk.p, s.part.p);
+        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
+                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, s.uk.p, s.part.p);
         if (!s.graph || s.graph_key != key) {
             if (s.graph) {
                 cudaGraphExecDestroy(s.graph);
@@ -701,6 +701,7 @@ int acu_set_option(acu_ctx* c, int option, int value)
         if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 or 1");
         c->opt_projector = value;
         return ACU_OK;
+
     }
     return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
 }
@@ -742,6 +743,11 @@ int acu_radon_dev_f64(acu_ctx* c, int S, const double* i, double* s) { return ru
 int acu_radon_adjoint_dev_f64(acu_ctx* c, int S, const double* s, double* i)
 {
     return run_op<double>(c, OP_RADON_ADJ, S, s, i);
+}
+int acu_filter_dev_f64(acu_ctx* c, int S, const double* s, double* o) { return run_op<double>(c, OP_FILTER, S, s, o); }
+int acu_backproject_dev_f64(acu_ctx* c, int S, const double* q, double* i)
+{
+    return run_op<double>(c, OP_BACKPROJECT, S, q, i);
 }
 
 int acu_tvopt(acu_ctx* c, int S, const float* f, int ninner, int nouter, int ncg, float lambda, float mu,

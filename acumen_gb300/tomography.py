@@ -136,21 +136,17 @@ class Tomography:
 
     def filter(self, sino):
         """First half of iradon: the ramp filter (tv_hpc.F90:93-105); CUDA tensors only."""
-        lead, S = self._shape_in(sino, "sino")
-        out = torch.empty_like(sino)
-        self._sync_stream()
-        call("acu_filter_dev", self._h, S, ctypes.c_void_p(sino.data_ptr()), ctypes.c_void_p(out.data_ptr()),
-             ctx=self._h)
-        return out
+        return self._op("acu_filter", self._cuda_only(sino), "sino", "sino")
 
     def backproject(self, filtered):
         """Second half of iradon (tv_hpc.F90:107-123); CUDA tensors only."""
-        lead, S = self._shape_in(filtered, "sino")
-        out = torch.empty(lead + (self.nimage, self.nimage), dtype=filtered.dtype, device=filtered.device)
-        self._sync_stream()
-        call("acu_backproject_dev", self._h, S, ctypes.c_void_p(filtered.data_ptr()),
-             ctypes.c_void_p(out.data_ptr()), ctx=self._h)
-        return out
+        return self._op("acu_backproject", self._cuda_only(filtered), "sino", "img")
+
+    @staticmethod
+    def _cuda_only(x):
+        if not _is_cuda_tensor(x):
+            raise TypeError("filter and backproject take CUDA tensors (float32 or float64)")
+        return x
 
     def tvopt(self, f, ninner: int, nouter: int, ncg: int, lam: float, mu: float, plain: bool = False):
         """tomography/tv_hpc.F90:162-363: returns (tv, fbp).  plain=True runs

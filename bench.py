@@ -57,6 +57,8 @@ def parse():
     ap.add_argument("--op", default=None, choices=[None, "radon", "iradon", "backproject", "filter", "tvstep"],
                     help="time one operator on the workload's batch (used for ncu captures)")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--option", action="append", default=[], metavar="ID=VALUE",
+                    help="set a context option (acu_set_option) before running, e.g. 8=1")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e / plain / FBP / CPU legs")
     return ap.parse_args()
 
@@ -373,6 +375,9 @@ def main():
     N, T, S = args.size, args.angles, args.slices
     th, f = make_batch(S, N, T, "cuda")
     t = Tomography(N, th, WPU)
+    for o in args.option:
+        k, v = o.split("=")
+        t.set_option(int(k), int(v))
     if args.op:
         return run_op(args, t, f, S)
 

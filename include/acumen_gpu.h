@@ -89,6 +89,8 @@ int acu_backproject_dev(acu_ctx *ctx, int nslices, const float *d_filtered, floa
 int acu_iradon_dev_f64(acu_ctx *ctx, int nslices, const double *d_sino, double *d_img);
 int acu_radon_dev_f64(acu_ctx *ctx, int nslices, const double *d_img, double *d_sino);
 int acu_radon_adjoint_dev_f64(acu_ctx *ctx, int nslices, const double *d_sino, double *d_img);
+int acu_filter_dev_f64(acu_ctx *ctx, int nslices, const double *d_sino, double *d_out);
+int acu_backproject_dev_f64(acu_ctx *ctx, int nslices, const double *d_filtered, double *d_img);
 
 /* ---- split-Bregman TV: tomography/tv_hpc.F90:162-363 (tvopt) ---------------
  * Solves every slice of f (S*T*N) with ninner x nouter Bregman iterations of

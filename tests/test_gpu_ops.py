@@ -90,6 +90,16 @@ def test_filter_and_backproject_halves(case, oracle):
     assert rel(q_fft, ref) < 1e-5
     img = t.backproject(q_dir)
     assert rel(img, oracle.backproject(q_dir.cpu().numpy().astype(np.float64), case["th"], case["wpu"], 64)) < 1e-6
+    # double precision halves against the FP64 oracle
+    s64 = sino.double()
+    for filt in (0, 1):
+        t.set_option(1, filt)
+        q64 = t.filter(s64)
+        assert q64.dtype == torch.float64 and rel(q64, oracle.filter_rows(s64.cpu().numpy(), 64)) < 1e-11
+    img64 = t.backproject(q64)
+    assert rel(img64, oracle.backproject(q64.cpu().numpy(), case["th"], case["wpu"], 64)) < 1e-11
+    with pytest.raises(TypeError):
+        t.backproject(q64.cpu().numpy())
 
 
 @pytest.mark.parametrize("S", [1, 4])
@@ -162,3 +172,4 @@ def test_projector_variants_agree(case, oracle):
         ref = oracle.radon(x, case["th"], 32)
         for o in outs:
             assert rel(o, ref) < 1e-6
+

@@ -123,3 +123,19 @@ def test_fp32_tracks_fp64_at_larger_size(built_lib):
     tv64, _ = t.tvopt(f.double(), 1, 20, 10, 0.05, 1.0)
     mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0].cpu().numpy()
     assert rel(tv32, tv64, mask) < TV_TOL
+
+
+def test_graph_follows_projector_option(prob):
+    """A captured outer iteration is rebuilt when the projector variant
+    changes: switching a context to variant 0 gives exactly what a context
+    created with variant 0 gives."""
+    a = prob["args"]
+    f = torch.from_numpy(prob["f"][:4]).cuda()
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    t.set_option(7, 0)
+    tv0, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    u = Tomography(prob["N"], prob["th"], prob["wpu"])
+    u.set_option(7, 0)
+    ref0, _ = u.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    assert torch.equal(tv0, ref0)
