@@ -92,6 +92,7 @@ SIGNATURES = {
     "acu_batch_tvopt": [P, P, I, I, I, F, F, P, P],
     "acu_batch_op": [P, I, P, P],
     "acu_batch_tuning": [P, ctypes.POINTER(I), ctypes.POINTER(I)],
+    "acu_batch_set_option": [P, I, I],
     "acu_tv_loss_grad_dev_f64": [P, I, P, P, P, D, D, P, P, P],
 }
 

@@ -88,3 +88,7 @@ class RaggedBatch:
         w, r = ctypes.c_int(), ctypes.c_int()
         self._check(lib().acu_batch_tuning(self._h, ctypes.byref(w), ctypes.byref(r)))
         return w.value, r.value
+
+    def set_option(self, option, value):
+        """acu_batch_set_option: ACU_OPT_POSITIONS (8) only."""
+        self._check(lib().acu_batch_set_option(self._h, int(option), int(value)))

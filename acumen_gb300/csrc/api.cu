@@ -57,6 +57,10 @@ int ensure_geom(acu_ctx* c)
     CK(c, gs.fft_tw.ensure(sizeof(double) * h.fft_tw.size()));
     CK(c, cudaMemcpy(gs.sc_bp.p, h.sc_bp.data(), sizeof(Real) * h.sc_bp.size(), cudaMemcpyHostToDevice));
     CK(c, cudaMemcpy(gs.sc_fp.p, h.sc_fp.data(), sizeof(Real) * h.sc_fp.size(), cudaMemcpyHostToDevice));
+    CK(c, gs.xsc_bp.ensure(sizeof(float) * h.xsc_bp.size()));
+    CK(c, gs.xsc_fp.ensure(sizeof(float) * h.xsc_fp.size()));
+    CK(c, cudaMemcpy(gs.xsc_bp.p, h.xsc_bp.data(), sizeof(float) * h.xsc_bp.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(gs.xsc_fp.p, h.xsc_fp.data(), sizeof(float) * h.xsc_fp.size(), cudaMemcpyHostToDevice));
     CK(c, cudaMemset(gs.filt.p, 0, sizeof(Real) * (h.filt.size() + 8)));
     CK(c, cudaMemcpy(gs.filt.p, h.filt.data(), sizeof(Real) * h.filt.size(), cudaMemcpyHostToDevice));
     CK(c, cudaMemcpy(gs.cmask.p, h.cmask.data(), sizeof(Real) * h.cmask.size(), cudaMemcpyHostToDevice));
@@ -88,6 +92,9 @@ int ensure_geom(acu_ctx* c)
         CK(c, cudaMemcpy(gs.fp_order.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
         gs.d.fp_order = gs.fp_order.template as<int>();
     }
+    gs.d.xsc_bp = gs.xsc_bp.template as<float4>();
+    gs.d.xsc_fp = gs.xsc_fp.template as<float4>();
+    gs.d.exact = (sizeof(Real) == 4) ? c->opt_positions : 0;
     gs.d.fft_L = h.fft_L;
     gs.d.fft_log2L = h.fft_log2L;
     gs.ready = true;
@@ -355,8 +362,8 @@ int tv_iterate_v(acu_ctx* c, int nouter)
     const bool use_graph = c->opt_graph != 0 && !run.verbose;
     if (use_graph) {
         char key[256];
-        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
-                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, s.uk.p, s.part.p);
+        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
+                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, s.uk.p, s.part.p);
         if (!s.graph || s.graph_key != key) {
             if (s.graph) {
                 cudaGraphExecDestroy(s.graph);
@@ -701,6 +708,11 @@ int acu_set_option(acu_ctx* c, int option, int value)
         if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 or 1");
         c->opt_projector = value;
         return ACU_OK;
+    case 8:
+        if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_POSITIONS must be 0 or 1");
+        c->opt_positions = value;
+        c->g32.d.exact = value;
+        return ACU_OK;
 
     }
     return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
@@ -717,6 +729,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case ACU_OPT_PRINT_EVERY: *value = c->opt_print_every; return ACU_OK;
     case 6: *value = c->opt_slice_base; return ACU_OK;
     case 7: *value = c->opt_projector; return ACU_OK;
+    case 8: *value = c->opt_positions; return ACU_OK;
     }
     return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);
 }

@@ -25,28 +25,23 @@ namespace acu {
 
 // One staggered ray of the single-slice projector (as radon_stag_ray<1> in
 // kernels_radon.cu).
+template <bool EX>
 __device__ __forceinline__ void radon_stag_ray_v1(const float* __restrict__ I, const float* __restrict__ IT, int N,
-                                                  float s, float c, float mid, int jy, int lane, bool transposed,
-                                                  float (&acc)[1])
+                                                  float s, float c, const ProjRay<float, EX>& ray, float mid, int jy,
+                                                  int lane, bool transposed, float (&acc)[1])
 {
     const float ratio = transposed ? -s / c : c / s;
     const int kb = __float2int_rn((float)lane * ratio);
     const int kend = __float2int_rn(31.f * ratio);
     const int kmin = min(0, kend), kmax = max(0, kend);
-    const float dyv = (float)jy - mid;
-    const float sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
     const float* base = transposed ? IT : I;
     for (int i = 1 + kmin; i <= N + kmax; ++i) {
         const int jx = i - kb;
         if (jx < 1 || jx > N || jy > N) continue;
-        const float dxv = (float)jx - mid;
-        const float xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
-        const float yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
-        const float x1f = floorf(xr), y1f = floorf(yr);
-        const int x1 = (int)x1f, y1 = (int)y1f;
+        int x1, y1;
+        float wxl, wxh, wyl, wyh;
+        ray.at((float)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
         if (min(x1, y1) > 1 && max(x1, y1) < N) {
-            const float wxl = add_rn(x1f, 1.f) - xr, wxh = xr - x1f;
-            const float wyl = add_rn(y1f, 1.f) - yr, wyh = yr - y1f;
             const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
             const int r0 = transposed ? x1 : y1, c0 = transposed ? y1 : x1;
             const float* q = base + (size_t)(r0 - 1) * N + (c0 - 1);
@@ -74,10 +69,11 @@ __device__ __forceinline__ int find_prob(const ProbDesc* __restrict__ pd, int np
 // ---- projector: one warp item = 32 rays of one angle of one problem --------
 // Staggered rays through the image or its transpose (whichever the warp's
 // rays spread along), as the uniform projector.
+template <bool EX>
 __global__ void __launch_bounds__(512) k_batch_radon(const ProbDesc* __restrict__ pd, int nprob,
                                                      const float* __restrict__ img, const float* __restrict__ IT,
                                                      float* __restrict__ sino, const float* __restrict__ sc,
-                                                     long long total, int* counter)
+                                                     const float4* __restrict__ xsc, long long total, int* counter)
 {
     const int lane = threadIdx.x & 31;
     for (;;) {
@@ -92,8 +88,9 @@ __global__ void __launch_bounds__(512) k_batch_radon(const ProbDesc* __restrict_
         const int jy = b * 32 + lane + 1;
         const int N = d.N;
         const float s = sc[d.sc + 2 * t], c = sc[d.sc + 2 * t + 1];
+        const ProjRay<float, EX> ray(sc + d.sc, xsc + d.sc / 2, t, jy, d.mid, nullptr);
         float acc[1] = {0.f};
-        radon_stag_ray_v1(img + d.img, IT + d.img, N, s, c, d.mid, jy, lane, fabsf(c) > fabsf(s), acc);
+        radon_stag_ray_v1<EX>(img + d.img, IT + d.img, N, s, c, ray, d.mid, jy, lane, fabsf(c) > fabsf(s), acc);
         if (jy <= N) sino[d.sino + (size_t)t * N + (jy - 1)] = acc[0] / (float)N;
     }
 }
@@ -123,9 +120,11 @@ __global__ void __launch_bounds__(256) k_batch_transpose(const ProbDesc* __restr
 }
 
 // ---- backprojection: one block item = a 32 x R pixel tile of one problem ----
+template <bool EX>
 __global__ void __launch_bounds__(512) k_batch_backproject(const ProbDesc* __restrict__ pd, int nprob,
                                                            const float* __restrict__ q, float* __restrict__ img,
                                                            const float* __restrict__ sc,
+                                                           const float4* __restrict__ xsc,
                                                            const float* __restrict__ cmask, long long total,
                                                            int* counter)
 {
@@ -153,13 +152,22 @@ __global__ void __launch_bounds__(512) k_batch_backproject(const ProbDesc* __res
             const float dx = (float)jx - mid, dy = (float)jy - mid;
             const float* qq = q + d.sino;
             const float* sct = sc + d.sc;
+            const float4* xst = xsc + d.sc / 2;
             for (int t = 0; t < d.T; ++t) {
-                const float s = sct[2 * t], c = sct[2 * t + 1];
-                const float yr = add_rn(add_rn(mul_rn(s, dx), mul_rn(c, dy)), mid);
-                const float y1f = floorf(yr);
+                float y1f, wl, wh;
+                if constexpr (EX) {
+                    const float4 x = __ldg(xst + t);
+                    exact_coord(x.x, x.y, x.z, x.w, dx, dy, mid, y1f, wh);
+                    wl = 1.f - wh;
+                } else {
+                    const float s = sct[2 * t], c = sct[2 * t + 1];
+                    const float yr = add_rn(add_rn(mul_rn(s, dx), mul_rn(c, dy)), mid);
+                    y1f = floorf(yr);
+                    wl = add_rn(y1f, 1.f) - yr;
+                    wh = yr - y1f;
+                }
                 const int y1 = (int)y1f;
                 if (y1 > 1 && y1 < N) {
-                    const float wl = add_rn(y1f, 1.f) - yr, wh = yr - y1f;
                     const float* row = qq + (size_t)t * N + (y1 - 1);
                     acc = fmaf(__ldg(row + 1), wh, fmaf(__ldg(row), wl, acc));
                 }
@@ -437,14 +445,24 @@ void batch_radon(const BatchDev& b, const float* img, float* sino, int slot, cud
     cudaMemsetAsync(b.counter + slot, 0, sizeof(int), st);
     const int threads = 32 * b.radon_warps;
     const int blocks = sm_count() * (2048 / threads);
-    k_batch_radon<<<blocks, threads, 0, st>>>(b.pd, b.nprob, img, b.IT, sino, b.sc_fp, b.n_radon, b.counter + slot);
+    if (b.exact)
+        k_batch_radon<true><<<blocks, threads, 0, st>>>(b.pd, b.nprob, img, b.IT, sino, b.sc_fp, b.xsc_fp, b.n_radon,
+                                                        b.counter + slot);
+    else
+        k_batch_radon<false><<<blocks, threads, 0, st>>>(b.pd, b.nprob, img, b.IT, sino, b.sc_fp, b.xsc_fp, b.n_radon,
+                                                         b.counter + slot);
 }
 void batch_backproject(const BatchDev& b, const float* q, float* img, int slot, cudaStream_t st)
 {
     cudaMemsetAsync(b.counter + slot, 0, sizeof(int), st);
     dim3 blk(32, b.bp_rows);
     const int blocks = sm_count() * (2048 / (32 * b.bp_rows));
-    k_batch_backproject<<<blocks, blk, 0, st>>>(b.pd, b.nprob, q, img, b.sc_bp, b.cmask, b.n_bp, b.counter + slot);
+    if (b.exact)
+        k_batch_backproject<true><<<blocks, blk, 0, st>>>(b.pd, b.nprob, q, img, b.sc_bp, b.xsc_bp, b.cmask, b.n_bp,
+                                                          b.counter + slot);
+    else
+        k_batch_backproject<false><<<blocks, blk, 0, st>>>(b.pd, b.nprob, q, img, b.sc_bp, b.xsc_bp, b.cmask, b.n_bp,
+                                                           b.counter + slot);
 }
 void batch_filter(const BatchDev& b, const float* sino, float* out, cudaStream_t st)
 {
@@ -509,7 +527,7 @@ struct acu_batch {
     std::vector<ProbDesc> desc;       // in caller order
     std::vector<int> order;           // execution order (largest work first) -> caller index
     BatchDev dev;
-    DevBuf d_pd, d_sc_bp, d_sc_fp, d_cm, d_fh, d_tw, d_counter;
+    DevBuf d_pd, d_sc_bp, d_sc_fp, d_xsc_bp, d_xsc_fp, d_cm, d_fh, d_tw, d_counter;
     DevBuf f, fk, ruk, rp, q, uk, dx, dy, bx, by, rhs, r, p, Ap, tmp, part, rsold, alpha, beta, it_img;
     DevBuf io_in, io_out;
     cudaGraphExec_t graph = nullptr;
@@ -650,7 +668,7 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
     if (2 * (size_t)Lmax * sizeof(float2) > 227 * 1024)
         return berr(b.get(), ACU_ERR_UNSUPPORTED, "a problem needs an FFT longer than 8192 (grid side > 4097)");
     b->desc.resize(nprob);
-    std::vector<float> sc_bp, sc_fp, cm, fh;
+    std::vector<float> sc_bp, sc_fp, xsc_bp, xsc_fp, cm, fh;
     long long img = 0, sino = 0, ir = 0, ib = 0, iff = 0, ie = 0, itr = 0;
     std::vector<ProbDesc> exec_desc;
     for (int k = 0; k < nprob; ++k) {
@@ -674,6 +692,8 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
         d.it_ew = ie;
         sc_bp.insert(sc_bp.end(), h.sc_bp.begin(), h.sc_bp.end());
         sc_fp.insert(sc_fp.end(), h.sc_fp.begin(), h.sc_fp.end());
+        xsc_bp.insert(xsc_bp.end(), h.xsc_bp.begin(), h.xsc_bp.end());   // 4 per angle: index sc / 2
+        xsc_fp.insert(xsc_fp.end(), h.xsc_fp.begin(), h.xsc_fp.end());
         cm.insert(cm.end(), h.cmask.begin(), h.cmask.end());
         fh.insert(fh.end(), h.fft_h.begin(), h.fft_h.end());
         img += (long long)d.N * d.N;
@@ -703,6 +723,8 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
     CKRET(up(b->d_pd, exec_desc.data(), sizeof(ProbDesc) * nprob));
     CKRET(up(b->d_sc_bp, sc_bp.data(), sizeof(float) * sc_bp.size()));
     CKRET(up(b->d_sc_fp, sc_fp.data(), sizeof(float) * sc_fp.size()));
+    CKRET(up(b->d_xsc_bp, xsc_bp.data(), sizeof(float) * xsc_bp.size()));
+    CKRET(up(b->d_xsc_fp, xsc_fp.data(), sizeof(float) * xsc_fp.size()));
     CKRET(up(b->d_cm, cm.data(), sizeof(float) * cm.size()));
     CKRET(up(b->d_fh, fh.data(), sizeof(float) * fh.size()));
     CKRET(up(b->d_tw, tw.data(), sizeof(float2) * tw.size()));
@@ -712,6 +734,8 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
     d.pd = b->d_pd.as<ProbDesc>();
     d.sc_bp = b->d_sc_bp.as<float>();
     d.sc_fp = b->d_sc_fp.as<float>();
+    d.xsc_bp = b->d_xsc_bp.as<float4>();
+    d.xsc_fp = b->d_xsc_fp.as<float4>();
     d.cmask = b->d_cm.as<float>();
     d.fft_h = b->d_fh.as<float>();
     d.tw = b->d_tw.as<float2>();
@@ -832,8 +856,8 @@ int batch_solve(acu_batch* b, const float* d_f_exec, int ninner, int nouter, int
     CKLAUNCH(c);
     if (nouter > 0) {
         char key[160];
-        snprintf(key, sizeof key, "%d/%d/%.9g/%.9g/%d/%d", ninner, ncg, (double)lambda, (double)mu, d.radon_warps,
-                 d.bp_rows);
+        snprintf(key, sizeof key, "%d/%d/%.9g/%.9g/%d/%d/%d", ninner, ncg, (double)lambda, (double)mu, d.radon_warps,
+                 d.bp_rows, d.exact);
         if (!b->graph || b->graph_key != key) {
             if (b->graph) {
                 cudaGraphExecDestroy(b->graph);
@@ -916,6 +940,15 @@ int acu_batch_tuning(const acu_batch* b, int* radon_warps, int* bp_rows)
     if (!b || !radon_warps || !bp_rows) return set_err(nullptr, ACU_ERR_INVALID, "null argument");
     *radon_warps = b->dev.radon_warps;
     *bp_rows = b->dev.bp_rows;
+    return ACU_OK;
+}
+
+int acu_batch_set_option(acu_batch* b, int option, int value)
+{
+    if (!b) return set_err(nullptr, ACU_ERR_INVALID, "null batch");
+    if (option != ACU_OPT_POSITIONS) return berr(b, ACU_ERR_INVALID, "acu_batch_set_option: only ACU_OPT_POSITIONS");
+    if (value != 0 && value != 1) return berr(b, ACU_ERR_INVALID, "ACU_OPT_POSITIONS must be 0 or 1");
+    b->dev.exact = value;
     return ACU_OK;
 }
 

@@ -142,4 +142,95 @@ __device__ __forceinline__ double block_sum(double v, double* sh /* >= 32 */)
     return r;
 }
 
+// cell = floor(hi + lo) and frac = (hi + lo) - cell for an exact high part
+// and a low part of a few cells at most, without forming hi + lo (whose
+// rounding at |hi| ~ 1e3 would be ~1e-4).
+__device__ __forceinline__ void split_floor(float hi, float lo, float& cell, float& frac)
+{
+    const float fl = floorf(hi);
+    const float fr = __fadd_rn(__fsub_rn(hi, fl), lo);
+    const float f2 = floorf(fr);
+    cell = __fadd_rn(fl, f2);
+    frac = __fsub_rn(fr, f2);
+}
+
+// Exact sample coordinate v = a*k1 + b*k2 + mid for integer-valued offsets
+// k1, k2 and coefficients split as a = a_hi + a_lo, b = b_hi + b_lo (a_hi,
+// b_hi multiples of 2^-q with q chosen on the host so that every partial sum
+// of the high part fits in 24 bits).  The high part is then exact, the low
+// part is below one cell, and the returned cell = floor(v) and frac = v -
+// cell are correct to ~1e-7 (host tables: tables.cpp).  A value the high
+// part cannot hold exactly lies outside the grid, before and after rounding.
+__device__ __forceinline__ void exact_coord(float a_hi, float b_hi, float a_lo, float b_lo, float k1, float k2,
+                                            float mid, float& cell, float& frac)
+{
+    split_floor(__fmaf_rn(a_hi, k1, __fmaf_rn(b_hi, k2, mid)), __fmaf_rn(a_lo, k1, __fmul_rn(b_lo, k2)), cell,
+                frac);
+}
+
+// Sample coordinates along one projector ray (tomography/tv_hpc.F90:144-146):
+//   xr = c*(jx-m) - s*dy + m,  yr = s*(jx-m) + c*dy + m,  dy = jy - m (+ off)
+// at(dx) returns the cells x1 = floor(xr), y1 = floor(yr) and the bilinear
+// weights wxl = x1+1-xr, wxh = xr-x1 (and the same in y).
+// EX = false: the reference's operation order in Real (single or double).
+// EX = true (single only): exact positions from the split FP64 tables.
+template <typename Real, bool EX>
+struct ProjRay {
+    Real s, c, sdy, cdy, mid;
+    __device__ ProjRay(const Real* sc, const float4*, int t, int jy, Real m, const Real* off_t) : mid(m)
+    {
+        s = sc[2 * t];
+        c = sc[2 * t + 1];
+        const Real dyv = off_t ? sub_rn(add_rn((Real)jy, *off_t), m) : (Real)jy - m;
+        sdy = mul_rn(s, dyv);
+        cdy = mul_rn(c, dyv);
+    }
+    __device__ __forceinline__ void at(Real dxv, int& x1, int& y1, Real& wxl, Real& wxh, Real& wyl, Real& wyh) const
+    {
+        const Real xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
+        const Real yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
+        const Real x1f = rfloor(xr), y1f = rfloor(yr);
+        x1 = (int)x1f;
+        y1 = (int)y1f;
+        wxl = add_rn(x1f, Real(1)) - xr;
+        wxh = xr - x1f;
+        wyl = add_rn(y1f, Real(1)) - yr;
+        wyh = yr - y1f;
+    }
+};
+
+template <>
+struct ProjRay<float, true> {
+    float sa, ca, sr, cr, bxh, byh, bxl, byl;
+    __device__ ProjRay(const float*, const float4* xsc, int t, int jy, float m, const float* off_t)
+    {
+        const float4 x = __ldg(xsc + t);
+        sa = x.x;
+        ca = x.y;
+        sr = x.z;
+        cr = x.w;
+        const float dy = (float)jy - m;
+        bxh = __fmaf_rn(-sa, dy, m);   // exact (see exact_coord)
+        byh = __fmaf_rn(ca, dy, m);
+        bxl = __fmul_rn(-sr, dy);
+        byl = __fmul_rn(cr, dy);
+        if (off_t) {                   // a detector offset joins the low part
+            const float o = *off_t;
+            bxl = __fmaf_rn(-sa, o, __fmaf_rn(-sr, o, bxl));
+            byl = __fmaf_rn(ca, o, __fmaf_rn(cr, o, byl));
+        }
+    }
+    __device__ __forceinline__ void at(float dx, int& x1, int& y1, float& wxl, float& wxh, float& wyl,
+                                       float& wyh) const
+    {
+        float cx, cy;
+        split_floor(__fmaf_rn(ca, dx, bxh), __fmaf_rn(cr, dx, bxl), cx, wxh);
+        split_floor(__fmaf_rn(sa, dx, byh), __fmaf_rn(sr, dx, byl), cy, wyh);
+        x1 = (int)cx;
+        y1 = (int)cy;
+        wxl = __fsub_rn(1.f, wxh);
+        wyl = __fsub_rn(1.f, wyh);
+    }
+};
+
 }  // namespace acu

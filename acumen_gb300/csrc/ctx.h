@@ -49,7 +49,7 @@ struct DevBuf {
 template <typename Real>
 struct GeomSet {
     bool ready = false;
-    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_tw, fp_order;
+    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_tw, fp_order, xsc_bp, xsc_fp;
     DevGeom<Real> d;
 };
 
@@ -84,6 +84,7 @@ struct acu_ctx {
     int opt_verbose = 0;
     int opt_print_every = 50;
     int opt_slice_base = 1;
+    int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions
     int opt_projector = 1;   // single-precision projector: 0 pair images, 1 lane image + transpose
     std::string err;
     acu::GeomSet<float> g32;

@@ -22,6 +22,11 @@ struct DevGeom {
     const double2* fft_tw64 = nullptr;
     int fft_L = 0, fft_log2L = 0;
     const int* fp_order = nullptr;  // [T] projector angles, |sin| >= |cos| first
+    // exact positions (single precision only): split FP64 angle tables,
+    // [T] x (s_a, c_a, s_r, c_r); exact != 0 selects them
+    const float4* xsc_bp = nullptr;
+    const float4* xsc_fp = nullptr;
+    int exact = 0;
 };
 
 // ---- radon operators (kernels_radon.cu); arrays in lane layout ------------

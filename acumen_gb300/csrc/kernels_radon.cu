@@ -57,10 +57,59 @@ __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
     st_lanes<Real, V>(img + ((size_t)g * N * N + pix) * V, acc);
 }
 
+// The same backprojection with exact sample positions (option 8): the
+// coordinate yr = s*dx + c*dy + mid is evaluated from the split FP64 angle
+// tables, so its cell and fraction agree with double precision to ~1e-7 px
+// instead of the ~1e-4 px of the reference's single-precision rounding at
+// grid sides of a few thousand.  Sums, weights and order are as above.
+template <int V>
+__global__ void __launch_bounds__(256) k_backproject_exact(const float* __restrict__ q,
+                                                           const float* __restrict__ cmask,
+                                                           const float4* __restrict__ xsc,
+                                                           float* __restrict__ img, int N, int T, float mid)
+{
+    const int jx = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int jy = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int g = blockIdx.z;
+    if (jx > N || jy > N) return;
+    const size_t pix = (size_t)(jy - 1) * N + (jx - 1);
+    const float cm = cmask[pix];
+    Lanes<float, V> acc;
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = 0.f;
+    if (cm != 0.f) {
+        const float dx = (float)jx - mid, dy = (float)jy - mid;
+        const float* qg = q + (size_t)g * T * N * V;
+        for (int t = 0; t < T; ++t) {
+            const float4 x = __ldg(xsc + t);
+            float cell, wh;
+            exact_coord(x.x, x.y, x.z, x.w, dx, dy, mid, cell, wh);
+            const int y1 = (int)cell;
+            if (y1 > 1 && y1 < N) {
+                const float wl = 1.f - wh;
+                const float* row = qg + ((size_t)t * N + (y1 - 1)) * V;
+                const Lanes<float, V> a = ld_lanes<float, V>(row);
+                const Lanes<float, V> b = ld_lanes<float, V>(row + V);
+#pragma unroll
+                for (int v = 0; v < V; ++v) acc.v[v] = fmaf(b.v[v], wh, fmaf(a.v[v], wl, acc.v[v]));
+            }
+        }
+    }
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc.v[v] = cm * acc.v[v];
+    st_lanes<float, V>(img + ((size_t)g * N * N + pix) * V, acc);
+}
+
 template <typename Real, int V>
 void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st)
 {
     dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G);
+    if constexpr (sizeof(Real) == 4) {
+        if (g.exact) {
+            k_backproject_exact<V><<<grd, blk, 0, st>>>(q, g.cmask, g.xsc_bp, img, g.N, g.T, g.mid);
+            return;
+        }
+    }
     k_backproject<Real, V><<<grd, blk, 0, st>>>(q, g.cmask, g.sc_bp, img, g.N, g.T, g.mid);
 }
 
@@ -74,33 +123,27 @@ void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img,
 // order.  The four bilinear weights are formed once per sample and shared by
 // the V slices.
 // ---------------------------------------------------------------------------
-template <typename Real, int V>
+template <typename Real, int V, bool EX>
 __global__ void __launch_bounds__(128) k_radon(const Real* __restrict__ img, const Real* __restrict__ sc,
-                                               Real* __restrict__ sino, int N, int T, Real mid,
-                                               const Real* __restrict__ off)
+                                               const float4* __restrict__ xsc, Real* __restrict__ sino, int N,
+                                               int T, Real mid, const Real* __restrict__ off)
 {
     const int jy = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int t = blockIdx.y * blockDim.y + threadIdx.y;
     const int g = blockIdx.z;
     if (jy > N || t >= T) return;
-    const Real s = sc[2 * t], c = sc[2 * t + 1];
     // bin jy is read at detector coordinate jy + off[t] (off: per-slice angle offsets, V = 1)
-    const Real dyv = off ? sub_rn(add_rn((Real)jy, off[(size_t)g * T + t]), mid) : (Real)jy - mid;
-    const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+    const ProjRay<Real, EX> ray(sc, xsc, t, jy, mid, off ? off + (size_t)g * T + t : nullptr);
     const Real* u = img + (size_t)g * N * N * V;
     const size_t rowstride = (size_t)N * V;
     Lanes<Real, V> acc;
 #pragma unroll
     for (int v = 0; v < V; ++v) acc.v[v] = Real(0);
     for (int jx = 1; jx <= N; ++jx) {
-        const Real dxv = (Real)jx - mid;
-        const Real xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
-        const Real yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
-        const Real x1f = rfloor(xr), y1f = rfloor(yr);
-        const int x1 = (int)x1f, y1 = (int)y1f;
+        int x1, y1;
+        Real wxl, wxh, wyl, wyh;
+        ray.at((Real)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
         if (min(x1, y1) > 1 && max(x1, y1) < N) {
-            const Real wxl = add_rn(x1f, Real(1)) - xr, wxh = xr - x1f;
-            const Real wyl = add_rn(y1f, Real(1)) - yr, wyh = yr - y1f;
             const Real w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
             const Real* p = u + ((size_t)(y1 - 1) * N + (x1 - 1)) * V;
             const Lanes<Real, V> a = ld_lanes<Real, V>(p);
@@ -121,7 +164,13 @@ template <typename Real, int V>
 void launch_radon(const DevGeom<Real>& g, int G, const Real* img, Real* sino, cudaStream_t st)
 {
     dim3 blk(32, 4), grd((g.N + 31) / 32, (g.T + 3) / 4, G);
-    k_radon<Real, V><<<grd, blk, 0, st>>>(img, g.sc_fp, sino, g.N, g.T, g.mid, nullptr);
+    if constexpr (sizeof(Real) == 4) {
+        if (g.exact) {
+            k_radon<Real, V, true><<<grd, blk, 0, st>>>(img, g.sc_fp, g.xsc_fp, sino, g.N, g.T, g.mid, nullptr);
+            return;
+        }
+    }
+    k_radon<Real, V, false><<<grd, blk, 0, st>>>(img, g.sc_fp, g.xsc_fp, sino, g.N, g.T, g.mid, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -187,14 +236,6 @@ __global__ void __launch_bounds__(256) k_make_pairs(const float* __restrict__ im
     }
 }
 
-// Each warp covers 8 adjacent rays x 4 interleaved step phases of one angle:
-// lane = ray (lane % 8) and phase (lane / 8); a lane sums the samples
-// jx = 1 + phase + 4k of its ray, and the four phase sums of a ray are added
-// with two butterfly shuffles ((p0 + p1) + (p2 + p3) in a fixed order).  The
-// 32 samples of one load instruction then form a compact 8 x 4 patch, which
-// touches fewer cache lines than 32 rays side by side.  Blocks take angles in
-// the order `order` (angles read through P first, then those read through
-// PT), so one pair image at a time is live in L2.
 // Staggered rays: a warp holds 32 adjacent rays of one angle and lane b walks
 // its own ray in the reference's order jx = 1..N, but started k_b =
 // rint(b * cos/sin) steps late (rint(-b * sin/cos) through the transposed
@@ -202,9 +243,11 @@ __global__ void __launch_bounds__(256) k_make_pairs(const float* __restrict__ im
 // two), 1 to 1.4 pixels apart.  A pair load of the warp then covers one or two
 // runs of consecutive pairs, the fewest cache lines 32 distinct samples can
 // touch.  Each ray's sum is sequential in jx, as in the reference.
+template <bool EX>
 __global__ void __launch_bounds__(128) k_radon_pairs(const float* __restrict__ P, const float* __restrict__ PT,
-                                                     const float* __restrict__ sc, const int* __restrict__ order,
-                                                     float* __restrict__ sino, int N, int T, float mid)
+                                                     const float* __restrict__ sc, const float4* __restrict__ xsc,
+                                                     const int* __restrict__ order, float* __restrict__ sino, int N,
+                                                     int T, float mid)
 {
     const int lane = threadIdx.x & 31;
     const int jy = blockIdx.x * 128 + threadIdx.y * 32 + lane + 1;
@@ -216,21 +259,16 @@ __global__ void __launch_bounds__(128) k_radon_pairs(const float* __restrict__ P
     const int kb = __float2int_rn((float)lane * ratio);
     const int kend = __float2int_rn(31.f * ratio);
     const int kmin = min(0, kend), kmax = max(0, kend);
-    const float dyv = (float)jy - mid;
-    const float sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+    const ProjRay<float, EX> ray(sc, xsc, t, jy, mid, nullptr);
     const float* base = (transposed ? PT : P) + (size_t)g * N * N * 8;
     float acc[4] = {0.f, 0.f, 0.f, 0.f};
     for (int i = 1 + kmin; i <= N + kmax; ++i) {
         const int jx = i - kb;
         if (jx < 1 || jx > N || jy > N) continue;
-        const float dxv = (float)jx - mid;
-        const float xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
-        const float yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
-        const float x1f = floorf(xr), y1f = floorf(yr);
-        const int x1 = (int)x1f, y1 = (int)y1f;
+        int x1, y1;
+        float wxl, wxh, wyl, wyh;
+        ray.at((float)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
         if (min(x1, y1) > 1 && max(x1, y1) < N) {
-            const float wxl = add_rn(x1f, 1.f) - xr, wxh = xr - x1f;
-            const float wyl = add_rn(y1f, 1.f) - yr, wyh = yr - y1f;
             const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
             const float* p = transposed ? base + ((size_t)(x1 - 1) * N + (y1 - 1)) * 8
                                         : base + ((size_t)(y1 - 1) * N + (x1 - 1)) * 8;
@@ -276,29 +314,23 @@ __global__ void __launch_bounds__(256) k_make_transpose(const float* __restrict_
 
 // One ray of the staggered projector, V slices per pixel (V = 1 or 4), read
 // from the copy selected by `transposed` (row = y1 in I, row = x1 in IT).
-template <int V>
+template <int V, bool EX>
 __device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, const float* __restrict__ IT, int N,
-                                               float s, float c, float mid, int jy, int lane, bool transposed,
-                                               float (&acc)[V])
+                                               float s, float c, const ProjRay<float, EX>& ray, float mid, int jy,
+                                               int lane, bool transposed, float (&acc)[V])
 {
     const float ratio = transposed ? -s / c : c / s;
     const int kb = __float2int_rn((float)lane * ratio);
     const int kend = __float2int_rn(31.f * ratio);
     const int kmin = min(0, kend), kmax = max(0, kend);
-    const float dyv = (float)jy - mid;
-    const float sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
     const float* base = transposed ? IT : I;
     for (int i = 1 + kmin; i <= N + kmax; ++i) {
         const int jx = i - kb;
         if (jx < 1 || jx > N || jy > N) continue;
-        const float dxv = (float)jx - mid;
-        const float xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
-        const float yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
-        const float x1f = floorf(xr), y1f = floorf(yr);
-        const int x1 = (int)x1f, y1 = (int)y1f;
+        int x1, y1;
+        float wxl, wxh, wyl, wyh;
+        ray.at((float)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
         if (min(x1, y1) > 1 && max(x1, y1) < N) {
-            const float wxl = add_rn(x1f, 1.f) - xr, wxh = xr - x1f;
-            const float wyl = add_rn(y1f, 1.f) - yr, wyh = yr - y1f;
             const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
             const int r0 = transposed ? x1 : y1, c0 = transposed ? y1 : x1;
             const float* p = base + ((size_t)(r0 - 1) * N + (c0 - 1)) * V;
@@ -315,10 +347,11 @@ __device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, cons
     }
 }
 
-template <int V>
+template <int V, bool EX>
 __global__ void __launch_bounds__(128) k_radon_stag(const float* __restrict__ I, const float* __restrict__ IT,
-                                                    const float* __restrict__ sc, const int* __restrict__ order,
-                                                    float* __restrict__ sino, int N, int T, float mid)
+                                                    const float* __restrict__ sc, const float4* __restrict__ xsc,
+                                                    const int* __restrict__ order, float* __restrict__ sino, int N,
+                                                    int T, float mid)
 {
     const int lane = threadIdx.x & 31;
     const int jy = blockIdx.x * 128 + threadIdx.y * 32 + lane + 1;
@@ -328,8 +361,9 @@ __global__ void __launch_bounds__(128) k_radon_stag(const float* __restrict__ I,
     float acc[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) acc[v] = 0.f;
-    radon_stag_ray<V>(I + (size_t)g * N * N * V, IT + (size_t)g * N * N * V, N, s, c, mid, jy, lane,
-                      fabsf(c) > fabsf(s), acc);
+    const ProjRay<float, EX> ray(sc, xsc, t, jy, mid, nullptr);
+    radon_stag_ray<V, EX>(I + (size_t)g * N * N * V, IT + (size_t)g * N * N * V, N, s, c, ray, mid, jy, lane,
+                          fabsf(c) > fabsf(s), acc);
     if (jy <= N) {
         Lanes<float, V> o;
 #pragma unroll
@@ -363,7 +397,10 @@ void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, floa
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, S);
     k_transpose_lanes<1><<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, S);
-    k_radon_stag<1><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    if (g.exact)
+        k_radon_stag<1, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    else
+        k_radon_stag<1, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
 }
 
 void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st)
@@ -371,7 +408,10 @@ void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float*
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
     k_make_transpose<<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, G);
-    k_radon_stag<4><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    if (g.exact)
+        k_radon_stag<4, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    else
+        k_radon_stag<4, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
 }
 
 void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float* P, float* PT, float* sino,
@@ -380,7 +420,10 @@ void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float*
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
     k_make_pairs<<<gp, bp, 0, st>>>(img, P, PT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, G);
-    k_radon_pairs<<<grd, blk, 0, st>>>(P, PT, g.sc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    if (g.exact)
+        k_radon_pairs<true><<<grd, blk, 0, st>>>(P, PT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    else
+        k_radon_pairs<false><<<grd, blk, 0, st>>>(P, PT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
 }
 
 // ---------------------------------------------------------------------------
@@ -390,9 +433,10 @@ void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float*
 // re-evaluated with the projector's own arithmetic, so cells and weights are
 // identical to the forward operator's.
 // ---------------------------------------------------------------------------
-template <typename Real, int V>
+template <typename Real, int V, bool EX>
 __global__ void __launch_bounds__(256) k_radon_adjoint(const Real* __restrict__ sino,
                                                        const Real* __restrict__ sc,
+                                                       const float4* __restrict__ xsc,
                                                        Real* __restrict__ img, int N, int T, Real mid,
                                                        const Real* __restrict__ off)
 {
@@ -411,7 +455,8 @@ __global__ void __launch_bounds__(256) k_radon_adjoint(const Real* __restrict__ 
             const Lanes<Real, 2> scp = ld_lanes<Real, 2>(sc + 2 * t);
             const Real s = scp.v[0], c = scp.v[1];
             // tap (px,py) of a sample at (xr,yr) means xr in [px-1,px+1), yr in [py-1,py+1)
-            const Real o = off ? off[(size_t)g * T + t] : Real(0);
+            const Real* off_t = off ? off + (size_t)g * T + t : nullptr;
+            const Real o = off ? *off_t : Real(0);
             const Real u = c * ex + s * ey + mid;       // jx of the sample at the pixel
             const Real w = -s * ex + c * ey + mid - o;  // jy
             int jx0 = (int)rfloor(u - Real(1.5)), jx1 = (int)rfloor(u + Real(1.5)) + 1;
@@ -419,19 +464,16 @@ __global__ void __launch_bounds__(256) k_radon_adjoint(const Real* __restrict__ 
             jx0 = max(jx0, 1); jy0 = max(jy0, 1); jx1 = min(jx1, N); jy1 = min(jy1, N);
             const Real* yt = yg + (size_t)t * N * V;
             for (int jy = jy0; jy <= jy1; ++jy) {
-                const Real dyv = off ? sub_rn(add_rn((Real)jy, o), mid) : (Real)jy - mid;
-                const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+                const ProjRay<Real, EX> ray(sc, xsc, t, jy, mid, off_t);
                 Real wsum = Real(0);
                 for (int jx = jx0; jx <= jx1; ++jx) {
-                    const Real dxv = (Real)jx - mid;
-                    const Real xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
-                    const Real yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
-                    const Real x1f = rfloor(xr), y1f = rfloor(yr);
-                    const int x1 = (int)x1f, y1 = (int)y1f;
+                    int x1, y1;
+                    Real wxl, wxh, wyl, wyh;
+                    ray.at((Real)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
                     if (min(x1, y1) > 1 && max(x1, y1) < N && (px == x1 || px == x1 + 1) &&
                         (py == y1 || py == y1 + 1)) {
-                        const Real wx = (px == x1) ? (add_rn(x1f, Real(1)) - xr) : (xr - x1f);
-                        const Real wy = (py == y1) ? (add_rn(y1f, Real(1)) - yr) : (yr - y1f);
+                        const Real wx = (px == x1) ? wxl : wxh;
+                        const Real wy = (py == y1) ? wyl : wyh;
                         wsum += wx * wy;
                     }
                 }
@@ -452,7 +494,13 @@ template <typename Real, int V>
 void launch_radon_adjoint(const DevGeom<Real>& g, int G, const Real* sino, Real* img, cudaStream_t st)
 {
     dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G);
-    k_radon_adjoint<Real, V><<<grd, blk, 0, st>>>(sino, g.sc_fp, img, g.N, g.T, g.mid, nullptr);
+    if constexpr (sizeof(Real) == 4) {
+        if (g.exact) {
+            k_radon_adjoint<Real, V, true><<<grd, blk, 0, st>>>(sino, g.sc_fp, g.xsc_fp, img, g.N, g.T, g.mid, nullptr);
+            return;
+        }
+    }
+    k_radon_adjoint<Real, V, false><<<grd, blk, 0, st>>>(sino, g.sc_fp, g.xsc_fp, img, g.N, g.T, g.mid, nullptr);
 }
 
 // ---------------------------------------------------------------------------
@@ -520,41 +568,48 @@ template <typename Real>
 void launch_radon_off(const DevGeom<Real>& g, int S, const Real* img, const Real* off, Real* sino, cudaStream_t st)
 {
     dim3 blk(32, 4), grd((g.N + 31) / 32, (g.T + 3) / 4, S);
-    k_radon<Real, 1><<<grd, blk, 0, st>>>(img, g.sc_fp, sino, g.N, g.T, g.mid, off);
+    if constexpr (sizeof(Real) == 4) {
+        if (g.exact) {
+            k_radon<Real, 1, true><<<grd, blk, 0, st>>>(img, g.sc_fp, g.xsc_fp, sino, g.N, g.T, g.mid, off);
+            return;
+        }
+    }
+    k_radon<Real, 1, false><<<grd, blk, 0, st>>>(img, g.sc_fp, g.xsc_fp, sino, g.N, g.T, g.mid, off);
 }
 template <typename Real>
 void launch_radon_adjoint_off(const DevGeom<Real>& g, int S, const Real* sino, const Real* off, Real* img,
                               cudaStream_t st)
 {
     dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, S);
-    k_radon_adjoint<Real, 1><<<grd, blk, 0, st>>>(sino, g.sc_fp, img, g.N, g.T, g.mid, off);
+    if constexpr (sizeof(Real) == 4) {
+        if (g.exact) {
+            k_radon_adjoint<Real, 1, true><<<grd, blk, 0, st>>>(sino, g.sc_fp, g.xsc_fp, img, g.N, g.T, g.mid, off);
+            return;
+        }
+    }
+    k_radon_adjoint<Real, 1, false><<<grd, blk, 0, st>>>(sino, g.sc_fp, g.xsc_fp, img, g.N, g.T, g.mid, off);
 }
 
 // D(jy,theta) = d/d(off) of the projector's value: (1/N) sum_jx of the
 // bilinear gradient along the detector direction, dB/dx * (-sin) + dB/dy * cos.
-template <typename Real>
+template <typename Real, bool EX>
 __global__ void __launch_bounds__(128) k_radon_doff(const Real* __restrict__ img, const Real* __restrict__ sc,
-                                                    Real* __restrict__ dsino, int N, int T, Real mid,
-                                                    const Real* __restrict__ off)
+                                                    const float4* __restrict__ xsc, Real* __restrict__ dsino, int N,
+                                                    int T, Real mid, const Real* __restrict__ off)
 {
     const int jy = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int t = blockIdx.y * blockDim.y + threadIdx.y;
     const int g = blockIdx.z;
     if (jy > N || t >= T) return;
     const Real s = sc[2 * t], c = sc[2 * t + 1];
-    const Real dyv = off ? sub_rn(add_rn((Real)jy, off[(size_t)g * T + t]), mid) : (Real)jy - mid;
-    const Real sdy = mul_rn(s, dyv), cdy = mul_rn(c, dyv);
+    const ProjRay<Real, EX> ray(sc, xsc, t, jy, mid, off ? off + (size_t)g * T + t : nullptr);
     const Real* u = img + (size_t)g * N * N;
     Real acc = Real(0);
     for (int jx = 1; jx <= N; ++jx) {
-        const Real dxv = (Real)jx - mid;
-        const Real xr = add_rn(sub_rn(mul_rn(c, dxv), sdy), mid);
-        const Real yr = add_rn(add_rn(mul_rn(s, dxv), cdy), mid);
-        const Real x1f = rfloor(xr), y1f = rfloor(yr);
-        const int x1 = (int)x1f, y1 = (int)y1f;
+        int x1, y1;
+        Real wxl, wxh, wyl, wyh;
+        ray.at((Real)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
         if (min(x1, y1) > 1 && max(x1, y1) < N) {
-            const Real wxl = add_rn(x1f, Real(1)) - xr, wxh = xr - x1f;
-            const Real wyl = add_rn(y1f, Real(1)) - yr, wyh = yr - y1f;
             const Real* p = u + (size_t)(y1 - 1) * N + (x1 - 1);
             const Real a = p[0], b = p[1], cc = p[N], d = p[N + 1];
             const Real gx = (b - a) * wyl + (d - cc) * wyh;
@@ -568,7 +623,13 @@ template <typename Real>
 void launch_radon_doff(const DevGeom<Real>& g, int S, const Real* img, const Real* off, Real* dsino, cudaStream_t st)
 {
     dim3 blk(32, 4), grd((g.N + 31) / 32, (g.T + 3) / 4, S);
-    k_radon_doff<Real><<<grd, blk, 0, st>>>(img, g.sc_fp, dsino, g.N, g.T, g.mid, off);
+    if constexpr (sizeof(Real) == 4) {
+        if (g.exact) {
+            k_radon_doff<Real, true><<<grd, blk, 0, st>>>(img, g.sc_fp, g.xsc_fp, dsino, g.N, g.T, g.mid, off);
+            return;
+        }
+    }
+    k_radon_doff<Real, false><<<grd, blk, 0, st>>>(img, g.sc_fp, g.xsc_fp, dsino, g.N, g.T, g.mid, off);
 }
 template void launch_radon_off<float>(const DevGeom<float>&, int, const float*, const float*, float*, cudaStream_t);
 template void launch_radon_off<double>(const DevGeom<double>&, int, const double*, const double*, double*,

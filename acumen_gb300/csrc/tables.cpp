@@ -70,6 +70,30 @@ void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& ou
         out.sc_fp[2 * t] = r_sin<Real>(ctf);
         out.sc_fp[2 * t + 1] = r_cos<Real>(ctf);
     }
+    // exact-position split (single-precision kernels, option 8): k = bits of
+    // mid bounds every pixel offset, q = 23 - k keeps s_a * offset and
+    // c_a * offset + mid within 24 significant bits
+    {
+        int k = 0;
+        while ((1L << k) <= (long)((N + 1) / 2)) ++k;
+        out.xq = 23 - k;
+        const double pid = 4.0 * std::atan(1.0);
+        out.xsc_bp.resize(4 * (size_t)T);
+        out.xsc_fp.resize(4 * (size_t)T);
+        auto split = [&](double v, float& a, float& r) {
+            const double av = std::ldexp(std::nearbyint(std::ldexp(v, out.xq)), -out.xq);
+            a = (float)av;
+            r = (float)(v - av);
+        };
+        for (int t = 0; t < T; ++t) {
+            const double th = (double)theta[t];
+            const double ctb = (pid * (90.0 - th)) / 180.0, ctf = (pid * (th - 90.0)) / 180.0;
+            split(std::sin(ctb), out.xsc_bp[4 * t], out.xsc_bp[4 * t + 2]);
+            split(std::cos(ctb), out.xsc_bp[4 * t + 1], out.xsc_bp[4 * t + 3]);
+            split(std::sin(ctf), out.xsc_fp[4 * t], out.xsc_fp[4 * t + 2]);
+            split(std::cos(ctf), out.xsc_fp[4 * t + 1], out.xsc_fp[4 * t + 3]);
+        }
+    }
     // FFT form of the same filter: circular kernel of length L >= 2N-2 holding
     // taps -(N-1)..(N-1) (the two taps +-(N-1) are equal and share one slot
     // when L = 2N-2); its DFT is real because the kernel is symmetric.

@@ -12,6 +12,12 @@ struct HostTables {
     std::vector<Real> cmask;   // N*N
     std::vector<Real> sc_bp;   // 2T
     std::vector<Real> sc_fp;   // 2T
+    // Exact-position split of the FP64 sines and cosines (both conventions):
+    // [T][4] = (s_a, c_a, s_r, c_r) with s_a a multiple of 2^-xq, so that
+    // s_a * k is exact in single precision for every pixel offset |k| <= mid,
+    // and s_r = s - s_a rounded to single precision.
+    std::vector<float> xsc_bp, xsc_fp;
+    int xq = 0;
     std::vector<Real> fft_h;   // L
     std::vector<double> fft_tw;  // 2*L: cos, sin of -2 pi k / L
     int fft_L = 0, fft_log2L = 0;

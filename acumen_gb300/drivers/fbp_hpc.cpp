@@ -30,6 +30,7 @@ int main()
         std::printf(" Reconstruction with Resolution: %d with %d projections\n", nimage, ntheta);
         acu_ctx* ctx = nullptr;
         check(acu_ctx_create(&ctx, nimage, ntheta, theta.data(), p.wpu), nullptr);
+        apply_positions(ctx);
         std::vector<std::unique_ptr<File>> fsino, frec;
         for (int k = 1; k <= fi.n_files_sino; ++k) fsino.emplace_back(new File(fnum(dir + "sinograms", k), false));
         for (int k = 1; k <= fi.n_files_rec; ++k) frec.emplace_back(new File(fnum(dir + "fbp", k), true));

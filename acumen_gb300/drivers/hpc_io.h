@@ -186,4 +186,14 @@ inline void check(int rc, acu_ctx* ctx)
     if (rc != ACU_OK) throw Fail(std::string("acumen_gpu: ") + acu_last_error(ctx));
 }
 
+// ACUMEN_POSITIONS=exact (or 1): single-precision sample positions from the
+// split FP64 angle tables (ACU_OPT_POSITIONS); default: the reference's.
+inline void apply_positions(acu_ctx* ctx)
+{
+    const std::string v = env("ACUMEN_POSITIONS", false);
+    if (v == "exact" || v == "1") check(acu_set_option(ctx, ACU_OPT_POSITIONS, 1), ctx);
+    else if (!v.empty() && v != "reference" && v != "0")
+        throw Fail("ACUMEN_POSITIONS must be 'reference' (0) or 'exact' (1), got '" + v + "'");
+}
+
 }  // namespace hpc

@@ -30,6 +30,7 @@ int main()
         std::printf(" Reconstruction with Resolution: %d with %d projections\n", nimage, ntheta);
         acu_ctx* ctx = nullptr;
         check(acu_ctx_create(&ctx, nimage, ntheta, theta.data(), p.wpu), nullptr);
+        apply_positions(ctx);
         check(acu_set_option(ctx, ACU_OPT_VERBOSE, 1), ctx);
         check(acu_set_option(ctx, ACU_OPT_PRINT_EVERY, 50), ctx);
         const bool sub = p.nsub + p.nsub_t != 2;

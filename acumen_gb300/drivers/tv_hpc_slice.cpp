@@ -22,6 +22,7 @@ int main()
         for (int jy = 1; jy <= ntheta; ++jy) theta[jy - 1] = f_theta[(jy - 1) * p.nsub_t + jts - 1];
         acu_ctx* ctx = nullptr;
         check(acu_ctx_create(&ctx, nimage, ntheta, theta.data(), p.wpu), nullptr);
+        apply_positions(ctx);
         check(acu_set_option(ctx, ACU_OPT_VERBOSE, 1), ctx);
         check(acu_set_option(ctx, ACU_OPT_PRINT_EVERY, 10), ctx);
         const int job_id = nimage / 2;                                         // :554

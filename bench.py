@@ -38,6 +38,7 @@ sys.path.insert(0, ROOT)
 METRIC = "TV slices/sec 2048²@1200 angles batched vs plain GPU at relL2≤1e-4; FBP GUPS"
 N_GRID, T_ANG, S_BATCH = 2049, 1200, 256
 NINNER, NCG, NOUTER, LAM, MU, WPU = 1, 10, 50, 0.05, 1.0, 100
+POSITIONS = {"reference": 0, "exact": 1}   # ACU_OPT_POSITIONS values
 # DRAM bytes (read + write) of one projector launch (k_radon_quads plus its
 # k_make_transpose) per group of 4 slices at 2049^2 x 1200 angles, from the ncu
 # capture summarised in profiles/k_radon_quads_2049sq_1200ang_4slices.md
@@ -54,9 +55,14 @@ def parse():
     ap.add_argument("--slices", type=int, default=S_BATCH)
     ap.add_argument("--size", type=int, default=N_GRID)
     ap.add_argument("--angles", type=int, default=T_ANG)
-    ap.add_argument("--op", default=None, choices=[None, "radon", "iradon", "backproject", "filter", "tvstep"],
-                    help="time one operator on the workload's batch (used for ncu captures)")
+    ap.add_argument("--op", default=None, choices=[None, "radon", "iradon", "backproject", "filter", "tvstep", "accuracy"],
+                    help="time one operator on the workload's batch (used for ncu captures); 'accuracy' prints the "
+                         "full FP64 comparison of both position modes")
     ap.add_argument("--reps", type=int, default=3)
+    ap.add_argument("--positions", default="exact", choices=["exact", "reference"],
+                    help="single-precision sample positions (ACU_OPT_POSITIONS): exact (split FP64 angle tables, "
+                         "the mode that meets relL2 <= 1e-4 against FP64 at the TV configurations) or the "
+                         "reference's single-precision arithmetic")
     ap.add_argument("--option", action="append", default=[], metavar="ID=VALUE",
                     help="set a context option (acu_set_option) before running, e.g. 8=1")
     ap.add_argument("--no-extras", action="store_true", help="skip e2e / plain / FBP / CPU legs")
@@ -207,11 +213,13 @@ def cpu_slices_per_s(N, T, threads=None):
 
 
 # ---------------------------------------------------------------------------
-def accuracy():
-    """Errors against FP64 at the configurations' full sizes.  The FP64 reference
+def accuracy(full=False):
+    """Errors against FP64 at the configurations' full sizes, for both
+    single-precision position modes (ACU_OPT_POSITIONS).  The FP64 reference
     here is the library's double-precision solver, itself checked against the
-    FP64 CPU oracle to 1e-9 at test sizes (tests/test_gpu_tv.py)."""
-    import numpy as np
+    FP64 CPU oracle to 1e-9 at test sizes (tests/test_gpu_tv.py).  full=True
+    (bench.py --op accuracy) adds one slice of the 2049^2 x 1200 workload and
+    the plain per-slice path; the FP64 solves take minutes there."""
     import torch
     from acumen_gb300 import synthetic as syn
     from acumen_gb300.tomography import Tomography
@@ -222,27 +230,41 @@ def accuracy():
             a, b = a[..., m], b[..., m]
         return float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
 
-    out = {}
-    # config 2: single-slice TV, 1449 grid (1448 bins made odd), 900 angles, I0 = 5e3, 50 x 10
-    N, T = 1449, 900
-    th = syn.angles(T)
-    f = syn.normalised_sinogram(syn.random_ellipses(2, 0.35 * N), N, th, I0=5e3, seed=2, device="cuda")[None]
-    t = Tomography(N, th, WPU)
-    tv32, fbp32 = t.tvopt(f.float(), NINNER, NOUTER, NCG, LAM, MU)
-    tv64, fbp64 = t.tvopt(f.double(), NINNER, NOUTER, NCG, LAM, MU)
-    tvp, _ = t.tvopt(f.float(), NINNER, NOUTER, NCG, LAM, MU, plain=True)
-    mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0]   # cmask support
-    out["config2_tv"] = {"rel_l2_disc_vs_fp64": rel(tv32, tv64, mask), "rel_l2_full_vs_fp64": rel(tv32, tv64),
-                         "plain_rel_l2_disc_vs_fp64": rel(tvp, tv64, mask),
-                         "fbp_rel_l2_vs_fp64": rel(fbp32, fbp64), "grid": N, "angles": T,
-                         "iterations": f"{NOUTER} x {NCG}"}
-    t.close()
+    def tv_case(N, T, seed, plain):
+        th = syn.angles(T)
+        f = syn.normalised_sinogram(syn.random_ellipses(seed, 0.35 * N), N, th, I0=5e3, seed=seed, device="cuda")[None]
+        t = Tomography(N, th, WPU)
+        tv64, fbp64 = t.tvopt(f.double(), NINNER, NOUTER, NCG, LAM, MU)
+        mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0]   # cmask support
+        t0 = time.perf_counter()
+        res = {"grid": N, "angles": T, "iterations": f"{NOUTER} x {NCG}"}
+        for name, pos in POSITIONS.items():
+            t.set_option(8, pos)
+            tv32, fbp32 = t.tvopt(f.float(), NINNER, NOUTER, NCG, LAM, MU)
+            r = {"rel_l2_disc_vs_fp64": rel(tv32, tv64, mask), "rel_l2_full_vs_fp64": rel(tv32, tv64),
+                 "fbp_rel_l2_vs_fp64": rel(fbp32, fbp64)}
+            if plain:
+                tvp, _ = t.tvopt(f.float(), NINNER, NOUTER, NCG, LAM, MU, plain=True)
+                r["plain_rel_l2_disc_vs_fp64"] = rel(tvp, tv64, mask)
+            res[name + "_positions"] = r
+        t.close()
+        res["seconds"] = time.perf_counter() - t0
+        return res
+
+    out = {"config2_tv": tv_case(1449, 900, 2, full)}           # single slice, 1448 bins made odd
+    if full:
+        out["config3_tv_one_slice"] = tv_case(N_GRID, T_ANG, 3, False)
     # config 1: FBP of 725^2 at 720 angles
     N, T = 725, 720
     th, ell, counts, flat, dark = syn.config1_sinogram(seed=1, device="cuda")
     p = (-torch.log(torch.clamp(counts - dark, min=1e-16) / max(flat - dark, 1.0))).float()[None]
     t = Tomography(N, th, WPU)
-    out["config1_fbp"] = {"rel_l2_vs_fp64": rel(t.iradon(p), t.iradon(p.double())), "grid": N, "angles": T}
+    fbp64 = t.iradon(p.double())
+    res = {"grid": N, "angles": T}
+    for name, pos in POSITIONS.items():
+        t.set_option(8, pos)
+        res[name + "_positions_rel_l2_vs_fp64"] = rel(t.iradon(p), fbp64)
+    out["config1_fbp"] = res
     t.close()
     return out
 
@@ -280,7 +302,7 @@ def pipeline(nproj=1200, ndet=2048, nrows=256, seed=3):
     return out
 
 
-def uneven_batch(nprob=64, seed=7):
+def uneven_batch(nprob=64, seed=7, positions=1):
     import numpy as np
     import torch
     from acumen_gb300 import synthetic as syn
@@ -293,6 +315,7 @@ def uneven_batch(nprob=64, seed=7):
     sinos = [syn.analytic_sinogram(syn.random_ellipses(500 + i, 0.5 * sd), N, th, device="cuda")
              .float().cpu().numpy() for i, (sd, N, th) in enumerate(zip(sides, Ns, ths))]
     b = RaggedBatch(Ns, ths, WPU)
+    b.set_option(8, positions)
     b.tvopt(sinos, NINNER, 1, NCG, LAM, MU)             # tuning, graph capture
     t0 = time.perf_counter()
     b.tvopt(sinos, NINNER, 1, NCG, LAM, MU)
@@ -336,6 +359,9 @@ def run_op(args, t, f, S):
     """One operator on the batch, for ncu captures and kernel timings."""
     import torch
     N = args.size
+    if args.op == "accuracy":
+        print(json.dumps(accuracy(full=True)), flush=True)
+        return
     if args.op == "radon":
         img = torch.rand(S, N, N, device="cuda")
         fn = lambda: t.radon(img)
@@ -375,6 +401,7 @@ def main():
     N, T, S = args.size, args.angles, args.slices
     th, f = make_batch(S, N, T, "cuda")
     t = Tomography(N, th, WPU)
+    t.set_option(8, POSITIONS[args.positions])
     for o in args.option:
         k, v = o.split("=")
         t.set_option(int(k), int(v))
@@ -420,6 +447,7 @@ def main():
                                    f"step = one outer iteration of the batch",
                        "global_batch": S * world, "seq_len": T, "parallelism": f"slices sharded, {world} rank(s)",
                        "l2": "inputs larger than L2 (batch state > 50 GB)",
+                       "positions": args.positions,
                        "t_warm_s": t_warm, "t_step_s": t_step},
             "clocks": clocks, "gpu_launches": kernel_launches * args.steps}
 
@@ -473,6 +501,7 @@ def main():
         # FBP GUPS: config 1 single slice (725^2, 720 angles) and the batch
         from acumen_gb300 import synthetic as syn
         t1c = Tomography(725, syn.angles(720), WPU)
+        t1c.set_option(8, POSITIONS[args.positions])
         s1 = torch.rand(1, 720, 725, device="cuda")
         g1 = 725 * 725 * 720 / cuda_time(lambda: t1c.iradon(s1), 10) / 1e9
         gb = N * N * T * S / cuda_time(lambda: t.iradon(f), 2) / 1e9
@@ -481,7 +510,7 @@ def main():
         # 180-1500 angles; one outer iteration timed as tvopt(2) - tvopt(1)
         del f
         torch.cuda.empty_cache()
-        line["uneven_batch"] = uneven_batch()
+        line["uneven_batch"] = uneven_batch(positions=POSITIONS[args.positions])
         line["pipeline"] = pipeline()
         line["accuracy"] = accuracy()
         # CPU baseline (bounded sample, all host cores)

@@ -65,6 +65,7 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_PRINT_EVERY 5 /* outer-loop period of those lines: 50 (tv_hpc) or 10 (tv_hpc_slice) */
 #define ACU_OPT_SLICE_BASE 6  /* slice number printed for the first slice of a call (default 1) */
 #define ACU_OPT_PROJECTOR 7   /* single-precision batched projector: 0 pair images, 1 image + transpose (default) */
+#define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 0 the reference's arithmetic (default), 1 exact */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
 
@@ -231,6 +232,9 @@ int acu_batch_tvopt(acu_batch *batch, const float *f, int ninner, int nouter, in
                     float *tv_out, float *fbp_out);
 int acu_batch_op(acu_batch *batch, int op, const float *in, float *out);
 int acu_batch_tuning(const acu_batch *batch, int *radon_warps, int *bp_rows);
+/* ACU_OPT_POSITIONS (0 or 1) for every problem of the batch; other options
+ * are rejected with ACU_ERR_INVALID. */
+int acu_batch_set_option(acu_batch *batch, int option, int value);
 
 /* ---- cross-correlation registration without device allocation --------------
  * No counterpart in the reference.  Same computation and results as

@@ -56,3 +56,29 @@ def test_batch_tv_matches_oracle(probs, oracle):
     tv2, _ = b.tvopt(probs["sinos"], 1, 4, 4, 0.05, 1.0)
     for a, c in zip(tv, tv2):
         np.testing.assert_array_equal(a, c)
+
+
+def test_batch_exact_positions(probs, oracle):
+    """ACU_OPT_POSITIONS on a ragged batch: the projector gives exactly what
+    the uniform single-slice path gives with the same option, both operators
+    stay within their bars of the FP64 oracle, and TV within 1e-4."""
+    from acumen_gb300.tomography import Tomography
+    b = RaggedBatch(probs["N"], probs["th"], probs["wpu"])
+    b.set_option(8, 1)
+    with pytest.raises(Exception):
+        b.set_option(1, 0)
+    r = b.radon(probs["imgs"])
+    ir = b.iradon(probs["sinos"])
+    for i, (img, s, th, N) in enumerate(zip(probs["imgs"], probs["sinos"], probs["th"], probs["N"])):
+        t = Tomography(N, th, probs["wpu"])
+        t.set_option(8, 1)
+        np.testing.assert_array_equal(r[i], t.radon(img.astype(np.float32)))
+        assert rel(r[i], oracle.radon(img, th, 64)) < 1e-6, i
+        assert rel(ir[i], t.iradon(s.astype(np.float32))) < 1e-6, i
+        assert rel(ir[i], oracle.iradon(s, th, probs["wpu"], 64)) < 1e-5, i
+        t.close()
+    tv, _ = b.tvopt(probs["sinos"], 1, 4, 4, 0.05, 1.0)
+    for i, (s, th, N) in enumerate(zip(probs["sinos"], probs["th"], probs["N"])):
+        ref_tv, _ = oracle.tvopt(s, th, probs["wpu"], 1, 4, 4, 0.05, 1.0, prec=64)
+        mask = oracle.cmask(N, len(th), probs["wpu"], 64) > 0
+        assert rel(tv[i], ref_tv, mask) < 1e-4, i

@@ -100,7 +100,15 @@ def test_pipeline_through_drivers(dataset, oracle):
     tw = th[jts - 1:jte]
     f = sino[:, jts - 1:jte, :]
     fbp = read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N)
-    assert rel(fbp, oracle.iradon(f.astype(np.float64), tw, 4, 64)) < 1e-5
+    ref_fbp64 = oracle.iradon(f.astype(np.float64), tw, 4, 64)
+    assert rel(fbp, ref_fbp64) < 1e-5
+    # ACUMEN_POSITIONS=exact selects the exact sample positions; a bad value fails
+    run("fbp_hpc", dict(env, ACUMEN_POSITIONS="exact"))
+    fbpx = read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N)
+    assert rel(fbpx, ref_fbp64) < 1e-5 and not np.array_equal(fbpx, fbp)
+    r = subprocess.run([os.path.join(B.BIN, "fbp_hpc")], env=dict(env, ACUMEN_POSITIONS="bogus"),
+                       capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0 and "ACUMEN_POSITIONS" in (r.stdout + r.stderr)
 
     # TV of every slice (tv_hpc), full resolution
     tenv = dict(env, Sub_Sample_Radial="1", Sub_Sample_Theta="1", Ninner_Loops="1", Nouter_Loops="3",

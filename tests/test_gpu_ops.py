@@ -173,3 +173,53 @@ def test_projector_variants_agree(case, oracle):
         for o in outs:
             assert rel(o, ref) < 1e-6
 
+
+
+def test_exact_positions_backprojection(oracle, built_lib):
+    """Option 8 = 1: backprojection sample positions from the split FP64 angle
+    tables.  On a ramp-filtered-like (high-pass) input at a 1025 grid, where
+    the reference's single-precision positions are off by ~6e-5 px, the exact
+    positions bring the result to single-precision round-off of the FP64
+    oracle."""
+    N, T, wpu = 1025, 300, 30
+    th = syn.angles(T)
+    q = np.random.default_rng(11).standard_normal((1, T, N)).astype(np.float32)
+    ref64 = oracle.backproject(q.astype(np.float64), th, wpu, 64)
+    t = Tomography(N, th, wpu)
+    qc = torch.from_numpy(q).cuda()
+    e_ref = rel(t.backproject(qc), ref64)
+    t.set_option(8, 1)
+    assert t.get_option(8) == 1
+    e_exact = rel(t.backproject(qc), ref64)
+    assert e_exact < 1e-6 and e_exact < e_ref / 5, (e_exact, e_ref)
+    # double precision ignores the option
+    assert rel(t.backproject(qc.double()), ref64) < 1e-11
+
+
+def test_exact_positions_projector_and_adjoint(oracle, built_lib):
+    """Option 8 = 1 for the projector variants, the single-slice path and the
+    exact adjoint: closer to the FP64 oracle than the reference's
+    single-precision positions on a random interior image at a 1025 grid,
+    and the adjoint pair still passes the dot-product test."""
+    N, T, wpu = 1025, 120, 30
+    th = syn.angles(T)
+    rng = np.random.default_rng(12)
+    x = rng.standard_normal((4, N, N)).astype(np.float32)
+    x[:, :3, :] = x[:, -3:, :] = x[:, :, :3] = x[:, :, -3:] = 0
+    ref64 = oracle.radon(x.astype(np.float64), th, 64)
+    t = Tomography(N, th, wpu)
+    xc = torch.from_numpy(x).cuda()
+    e_ref = rel(t.radon(xc), ref64)
+    t.set_option(8, 1)
+    for proj in (1, 0):
+        t.set_option(7, proj)
+        e4 = rel(t.radon(xc), ref64)                      # batched, 4 slices per thread
+        assert e4 < 3e-6 and e4 < e_ref / 5, (proj, e4, e_ref)
+    e1 = rel(t.radon(xc[:1]), ref64[:1])                  # single-slice staggered path
+    assert e1 < 3e-6 and e1 < e_ref / 5, e1
+    # dot-product test on positive data (no cancellation in either inner product)
+    xp = torch.from_numpy(rng.uniform(size=(4, N, N)).astype(np.float32)).cuda()
+    y = torch.from_numpy(rng.uniform(size=(4, T, N)).astype(np.float32)).cuda()
+    lhs = torch.sum(t.radon(xp).double() * y.double()).item()
+    rhs = torch.sum(xp.double() * t.radon_adjoint(y).double()).item()
+    assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
