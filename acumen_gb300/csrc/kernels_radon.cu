@@ -314,7 +314,7 @@ __global__ void __launch_bounds__(256) k_make_transpose(const float* __restrict_
 
 // One ray of the staggered projector, V slices per pixel (V = 1 or 4), read
 // from the copy selected by `transposed` (row = y1 in I, row = x1 in IT).
-template <int V, bool EX>
+template <int V, bool EX, bool PAR>
 __device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, const float* __restrict__ IT, int N,
                                                float s, float c, const ProjRay<float, EX>& ray, float mid, int jy,
                                                int lane, bool transposed, float (&acc)[V])
@@ -334,20 +334,39 @@ __device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, cons
             const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
             const int r0 = transposed ? x1 : y1, c0 = transposed ? y1 : x1;
             const float* p = base + ((size_t)(r0 - 1) * N + (c0 - 1)) * V;
-            // a = (r0, c0); b = (r0, c0+1); cc = (r0+1, c0); d = (r0+1, c0+1)
-            const Lanes<float, V> a = ld_lanes<float, V>(p);
-            const Lanes<float, V> b = ld_lanes<float, V>(p + V);
-            const Lanes<float, V> cc = ld_lanes<float, V>(p + (size_t)N * V);
-            const Lanes<float, V> d = ld_lanes<float, V>(p + (size_t)N * V + V);
             const float wb = transposed ? w12 : w21, wc = transposed ? w21 : w12;
+            if constexpr (PAR) {
+                // Rows by parity: the odd row of {r0, r0+1} first, then the
+                // even one.  The warp's samples straddle at most two cells
+                // (rows R and R+1), so one of the two row loads is the same
+                // row for every lane.
+                const bool odd = (r0 & 1) != 0;
+                const float* pA = odd ? p : p + (size_t)N * V;
+                const float* pB = odd ? p + (size_t)N * V : p;
+                const float wA0 = odd ? w11 : wc, wA1 = odd ? wb : w22;
+                const float wB0 = odd ? wc : w11, wB1 = odd ? w22 : wb;
+                const Lanes<float, V> a0 = ld_lanes<float, V>(pA);
+                const Lanes<float, V> a1 = ld_lanes<float, V>(pA + V);
+                const Lanes<float, V> b0 = ld_lanes<float, V>(pB);
+                const Lanes<float, V> b1 = ld_lanes<float, V>(pB + V);
 #pragma unroll
-            for (int v = 0; v < V; ++v)
-                acc[v] = fmaf(d.v[v], w22, fmaf(cc.v[v], wc, fmaf(b.v[v], wb, fmaf(a.v[v], w11, acc[v]))));
+                for (int v = 0; v < V; ++v)
+                    acc[v] = fmaf(b1.v[v], wB1, fmaf(b0.v[v], wB0, fmaf(a1.v[v], wA1, fmaf(a0.v[v], wA0, acc[v]))));
+            } else {
+                // a = (r0, c0); b = (r0, c0+1); cc = (r0+1, c0); d = (r0+1, c0+1)
+                const Lanes<float, V> a = ld_lanes<float, V>(p);
+                const Lanes<float, V> b = ld_lanes<float, V>(p + V);
+                const Lanes<float, V> cc = ld_lanes<float, V>(p + (size_t)N * V);
+                const Lanes<float, V> d = ld_lanes<float, V>(p + (size_t)N * V + V);
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    acc[v] = fmaf(d.v[v], w22, fmaf(cc.v[v], wc, fmaf(b.v[v], wb, fmaf(a.v[v], w11, acc[v]))));
+            }
         }
     }
 }
 
-template <int V, bool EX>
+template <int V, bool EX, bool PAR>
 __global__ void __launch_bounds__(128) k_radon_stag(const float* __restrict__ I, const float* __restrict__ IT,
                                                     const float* __restrict__ sc, const float4* __restrict__ xsc,
                                                     const int* __restrict__ order, float* __restrict__ sino, int N,
@@ -362,8 +381,8 @@ __global__ void __launch_bounds__(128) k_radon_stag(const float* __restrict__ I,
 #pragma unroll
     for (int v = 0; v < V; ++v) acc[v] = 0.f;
     const ProjRay<float, EX> ray(sc, xsc, t, jy, mid, nullptr);
-    radon_stag_ray<V, EX>(I + (size_t)g * N * N * V, IT + (size_t)g * N * N * V, N, s, c, ray, mid, jy, lane,
-                          fabsf(c) > fabsf(s), acc);
+    radon_stag_ray<V, EX, PAR>(I + (size_t)g * N * N * V, IT + (size_t)g * N * N * V, N, s, c, ray, mid, jy, lane,
+                               fabsf(c) > fabsf(s), acc);
     if (jy <= N) {
         Lanes<float, V> o;
 #pragma unroll
@@ -398,20 +417,28 @@ void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, floa
     k_transpose_lanes<1><<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, S);
     if (g.exact)
-        k_radon_stag<1, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+        k_radon_stag<1, true, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
     else
-        k_radon_stag<1, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+        k_radon_stag<1, false, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
 }
 
-void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st)
+void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st,
+                        bool par)
 {
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
     k_make_transpose<<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, G);
-    if (g.exact)
-        k_radon_stag<4, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
-    else
-        k_radon_stag<4, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    if (par) {
+        if (g.exact)
+            k_radon_stag<4, true, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+        else
+            k_radon_stag<4, false, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    } else {
+        if (g.exact)
+            k_radon_stag<4, true, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+        else
+            k_radon_stag<4, false, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    }
 }
 
 void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float* P, float* PT, float* sino,
