@@ -85,7 +85,8 @@ struct acu_ctx {
     int opt_print_every = 50;
     int opt_slice_base = 1;
     int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions
-    int opt_projector = 2;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 the same with row-parity loads
+    int opt_projector = 3;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 the same with
+                             // row-parity loads, 3 the same with taps reused from the previous sample
     std::string err;
     acu::GeomSet<float> g32;
     acu::GeomSet<double> g64;

@@ -366,6 +366,107 @@ __device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, cons
     }
 }
 
+// The same ray with the taps of the previous sample kept in registers.  A
+// lane's consecutive samples move by (cos, sin) (at most one cell per axis),
+// and the rows of the copy advance in one direction per angle (DIR, uniform
+// over the block).  When the cell is unchanged no tap is loaded; when only
+// the row advanced the shared row is reused and two taps are loaded; any
+// other move loads all four.  Values and summation order are those of
+// radon_stag_ray<V, EX, false>, so the results are identical.
+template <int V, bool EX, int DIR>
+__device__ __forceinline__ void radon_stag_ray_reuse(const float* __restrict__ base, int N, int kb, int kmin,
+                                                     int kmax, const ProjRay<float, EX>& ray, float mid, int jy,
+                                                     bool transposed, float (&acc)[V])
+{
+    int pr = -4, pc = -4;          // cell of the taps held (none yet)
+    Lanes<float, V> a, b, cc, d;   // (pr,pc) (pr,pc+1) (pr+1,pc) (pr+1,pc+1)
+#pragma unroll
+    for (int v = 0; v < V; ++v) a.v[v] = b.v[v] = cc.v[v] = d.v[v] = 0.f;
+    const size_t NV = (size_t)N * V;
+    for (int i = 1 + kmin; i <= N + kmax; ++i) {
+        const int jx = i - kb;
+        if (jx < 1 || jx > N || jy > N) continue;
+        int x1, y1;
+        float wxl, wxh, wyl, wyh;
+        ray.at((float)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
+        if (min(x1, y1) > 1 && max(x1, y1) < N) {
+            const float w11 = wxl * wyl, w21 = wxh * wyl, w12 = wxl * wyh, w22 = wxh * wyh;
+            const int r0 = transposed ? x1 : y1, c0 = transposed ? y1 : x1;
+            const float* p = base + ((size_t)(r0 - 1) * N + (c0 - 1)) * V;
+            const bool same = (c0 == pc) && (r0 == pr);
+            const bool shift = (c0 == pc) && (r0 == pr + DIR);
+            if constexpr (DIR > 0) {
+                if (shift) {
+                    a = cc;
+                    b = d;
+                }
+                if (!same && !shift) {
+                    a = ld_lanes<float, V>(p);
+                    b = ld_lanes<float, V>(p + V);
+                }
+                if (!same) {
+                    cc = ld_lanes<float, V>(p + NV);
+                    d = ld_lanes<float, V>(p + NV + V);
+                }
+            } else {
+                if (shift) {
+                    cc = a;
+                    d = b;
+                }
+                if (!same && !shift) {
+                    cc = ld_lanes<float, V>(p + NV);
+                    d = ld_lanes<float, V>(p + NV + V);
+                }
+                if (!same) {
+                    a = ld_lanes<float, V>(p);
+                    b = ld_lanes<float, V>(p + V);
+                }
+            }
+            pr = r0;
+            pc = c0;
+            const float wb = transposed ? w12 : w21, wc = transposed ? w21 : w12;
+#pragma unroll
+            for (int v = 0; v < V; ++v)
+                acc[v] = fmaf(d.v[v], w22, fmaf(cc.v[v], wc, fmaf(b.v[v], wb, fmaf(a.v[v], w11, acc[v]))));
+        }
+    }
+}
+
+template <int V, bool EX>
+__global__ void __launch_bounds__(128) k_radon_stag_reuse(const float* __restrict__ I, const float* __restrict__ IT,
+                                                          const float* __restrict__ sc,
+                                                          const float4* __restrict__ xsc,
+                                                          const int* __restrict__ order, float* __restrict__ sino,
+                                                          int N, int T, float mid)
+{
+    const int lane = threadIdx.x & 31;
+    const int jy = blockIdx.x * 128 + threadIdx.y * 32 + lane + 1;
+    const int t = order[blockIdx.y];
+    const int g = blockIdx.z;
+    const float s = sc[2 * t], c = sc[2 * t + 1];
+    const bool transposed = fabsf(c) > fabsf(s);
+    const float ratio = transposed ? -s / c : c / s;
+    const int kb = __float2int_rn((float)lane * ratio);
+    const int kend = __float2int_rn(31.f * ratio);
+    const int kmin = min(0, kend), kmax = max(0, kend);
+    const float* base = (transposed ? IT : I) + (size_t)g * N * N * V;
+    const ProjRay<float, EX> ray(sc, xsc, t, jy, mid, nullptr);
+    float acc[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) acc[v] = 0.f;
+    // the copy's rows follow y (step sin) in the image, x (step cos) in the transpose
+    if ((transposed ? c : s) >= 0.f)
+        radon_stag_ray_reuse<V, EX, 1>(base, N, kb, kmin, kmax, ray, mid, jy, transposed, acc);
+    else
+        radon_stag_ray_reuse<V, EX, -1>(base, N, kb, kmin, kmax, ray, mid, jy, transposed, acc);
+    if (jy <= N) {
+        Lanes<float, V> o;
+#pragma unroll
+        for (int v = 0; v < V; ++v) o.v[v] = acc[v] / (float)N;
+        st_lanes<float, V>(sino + (((size_t)g * T + t) * N + (jy - 1)) * V, o);
+    }
+}
+
 template <int V, bool EX, bool PAR>
 __global__ void __launch_bounds__(128) k_radon_stag(const float* __restrict__ I, const float* __restrict__ IT,
                                                     const float* __restrict__ sc, const float4* __restrict__ xsc,
@@ -423,12 +524,17 @@ void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, floa
 }
 
 void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st,
-                        bool par)
+                        bool par, bool reuse)
 {
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
     k_make_transpose<<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, G);
-    if (par) {
+    if (reuse) {
+        if (g.exact)
+            k_radon_stag_reuse<4, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+        else
+            k_radon_stag_reuse<4, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+    } else if (par) {
         if (g.exact)
             k_radon_stag<4, true, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
         else

@@ -65,7 +65,8 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_PRINT_EVERY 5 /* outer-loop period of those lines: 50 (tv_hpc) or 10 (tv_hpc_slice) */
 #define ACU_OPT_SLICE_BASE 6  /* slice number printed for the first slice of a call (default 1) */
 #define ACU_OPT_PROJECTOR 7   /* single-precision batched projector: 0 pair images, 1 image + transpose,
-                                 2 image + transpose with the taps loaded by row parity (default) */
+                                 2 the same with the taps loaded by row parity, 3 the same with the taps
+                                 of the previous sample reused (default) */
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 0 the reference's arithmetic (default), 1 exact */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
