@@ -261,17 +261,28 @@ struct TvRun {
 
     // One Bregman outer iteration (tv_hpc.F90:206-346).  On entry ruk holds
     // radon(uk) for the current uk, which the first inner iteration reuses.
+    bool merged = true;   // initial residual with one backprojection (ACU_OPT_RESIDUAL)
     void outer_body()
     {
         cudaStream_t st = c->stream;
         using E = TvEw<Real, V>;
         for (int jinner = 1; jinner <= ninner; ++jinner) {
             if (verbose) cudaMemcpyAsync(s->ukp.p, s->uk.p, sizeof(Real) * nimg(), cudaMemcpyDeviceToDevice, st);
-            iradon(B(s->fk), B(s->tmp));                                   // ifkt
-            E::rhs(N, G, mu, lambda, B(s->tmp), B(s->dx), B(s->bx), B(s->dy), B(s->by), B(s->rhs), st);
-            if (jinner > 1) radon(B(s->uk), B(s->ruk));
-            iradon(B(s->ruk), B(s->tmp));                                  // iukt
-            E::resid(N, G, mu, lambda, B(s->rhs), B(s->tmp), B(s->uk), B(s->r), B(s->p), sc, st);
+            if (merged) {
+                // mu*iradon(fk) - mu*iradon(radon(uk)) as one backprojection of
+                // the data residual fk - radon(uk) (iradon is linear)
+                if (jinner > 1) radon(B(s->uk), B(s->ruk));
+                E::diff(nsino(), B(s->fk), B(s->ruk), B(s->rp), st);
+                iradon(B(s->rp), B(s->tmp));
+                E::rhs(N, G, mu, lambda, B(s->tmp), B(s->dx), B(s->bx), B(s->dy), B(s->by), B(s->rhs), st);
+                E::resid(N, G, mu, lambda, B(s->rhs), nullptr, B(s->uk), B(s->r), B(s->p), sc, st);
+            } else {
+                iradon(B(s->fk), B(s->tmp));                               // ifkt
+                E::rhs(N, G, mu, lambda, B(s->tmp), B(s->dx), B(s->bx), B(s->dy), B(s->by), B(s->rhs), st);
+                if (jinner > 1) radon(B(s->uk), B(s->ruk));
+                iradon(B(s->ruk), B(s->tmp));                              // iukt
+                E::resid(N, G, mu, lambda, B(s->rhs), B(s->tmp), B(s->uk), B(s->r), B(s->p), sc, st);
+            }
             launch_cg_finalize(0, G * V, sc, st);
             for (int k = 0; k < ncg; ++k) {
                 radon(B(s->p), B(s->rp));
@@ -301,6 +312,7 @@ TvRun<Real, V> make_run(acu_ctx* c, TvState<Real>& s)
     run.N = c->N; run.T = c->T; run.G = s.G; run.S = s.S;
     run.ninner = s.ninner; run.ncg = s.ncg; run.lambda = (Real)s.lambda; run.mu = (Real)s.mu;
     run.verbose = c->opt_verbose != 0;
+    run.merged = c->opt_residual != 0;
     run.sc = TvScalars{s.rsold.template as<double>(), s.alpha.template as<double>(), s.beta.template as<double>(),
                        s.delta.template as<double>(), s.part.template as<double>(), s.nblk};
     return run;
@@ -364,8 +376,9 @@ int tv_iterate_v(acu_ctx* c, int nouter)
     const bool use_graph = c->opt_graph != 0 && !run.verbose;
     if (use_graph) {
         char key[256];
-        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
-                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, s.uk.p, s.part.p);
+        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
+                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, c->opt_residual, s.uk.p,
+                 s.part.p);
         if (!s.graph || s.graph_key != key) {
             if (s.graph) {
                 cudaGraphExecDestroy(s.graph);
@@ -715,6 +728,10 @@ int acu_set_option(acu_ctx* c, int option, int value)
         c->opt_positions = value;
         c->g32.d.exact = value;
         return ACU_OK;
+    case 9:
+        if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_RESIDUAL must be 0 or 1");
+        c->opt_residual = value;
+        return ACU_OK;
 
     }
     return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
@@ -732,6 +749,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case 6: *value = c->opt_slice_base; return ACU_OK;
     case 7: *value = c->opt_projector; return ACU_OK;
     case 8: *value = c->opt_positions; return ACU_OK;
+    case 9: *value = c->opt_residual; return ACU_OK;
     }
     return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);
 }

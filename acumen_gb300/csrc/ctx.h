@@ -84,6 +84,7 @@ struct acu_ctx {
     int opt_verbose = 0;
     int opt_print_every = 50;
     int opt_slice_base = 1;
+    int opt_residual = 1;    // 1 initial CG residual from one backprojection of fk - radon(uk), 0 two (reference)
     int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions
     int opt_projector = 3;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 the same with
                              // row-parity loads, 3 the same with taps reused from the previous sample

@@ -99,7 +99,13 @@ __global__ void __launch_bounds__(EW_THREADS) k_resid(int N, Real mu, Real lambd
         const int x = (int)(i % N), y = (int)(i / N);
         const size_t ii = i * V + base;
         const Lanes<Real, V> L = lap5<Real, V>(uk, N, x, y, base);
-        const Lanes<Real, V> h = ld_lanes_rw<Real, V>(rhs + ii), a = ld_lanes_rw<Real, V>(iukt + ii);
+        const Lanes<Real, V> h = ld_lanes_rw<Real, V>(rhs + ii);
+        Lanes<Real, V> a;   // iukt == nullptr: rhs already holds mu * iradon(fk - radon(uk))
+        if (iukt)
+            a = ld_lanes_rw<Real, V>(iukt + ii);
+        else
+#pragma unroll
+            for (int v = 0; v < V; ++v) a.v[v] = Real(0);
         Lanes<Real, V> o;
 #pragma unroll
         for (int v = 0; v < V; ++v) {
@@ -329,6 +335,18 @@ void TvEw<Real, V>::fk_update(size_t n, Real* fk, const Real* f, const Real* ruk
 {
     size_t b = (n + 255) / 256;
     k_fk<Real><<<(unsigned)(b < 4096 ? b : 4096), 256, 0, st>>>(n, fk, f, ruk);
+}
+template <typename Real>
+__global__ void k_diff(size_t n, const Real* __restrict__ a, const Real* __restrict__ b, Real* __restrict__ out)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        out[i] = a[i] - b[i];
+}
+template <typename Real, int V>
+void TvEw<Real, V>::diff(size_t n, const Real* a, const Real* b, Real* out, cudaStream_t st)
+{
+    size_t nb = (n + 255) / 256;
+    k_diff<Real><<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, st>>>(n, a, b, out);
 }
 
 // ---- layout conversion -------------------------------------------------------

@@ -433,10 +433,12 @@ def main():
     value = job_value(world, S, t_warm, t_step)
     # kernels of one outer iteration (the captured graph): transpose + projector
     # per radon, filter + backprojection per iradon, and the element-wise /
-    # finaliser kernels (101 for ninner=1, ncg=10; the ncu launch list agrees)
+    # finaliser kernels (100 for ninner=1, ncg=10 with the merged initial
+    # residual, 101 with the reference's two backprojections)
+    merged = t.get_option(9) == 1
     n_radon = NINNER * NCG + (NINNER - 1) + 1
-    n_iradon = NINNER * (2 + NCG)
-    n_ew = NINNER * (4 + 5 * NCG) + 1
+    n_iradon = NINNER * ((1 if merged else 2) + NCG)
+    n_ew = NINNER * ((5 if merged else 4) + 5 * NCG) + 1
     kernel_launches = 2 * n_radon + 2 * n_iradon + n_ew
 
     line = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world, "steps": args.steps,

@@ -68,6 +68,8 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
                                  2 the same with the taps loaded by row parity, 3 the same with the taps
                                  of the previous sample reused (default) */
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 0 the reference's arithmetic (default), 1 exact */
+#define ACU_OPT_RESIDUAL 9    /* batched TV: the initial CG residual mu*iradon(fk) - mu*iradon(radon(uk)) as
+                                 1 one backprojection of fk - radon(uk) (default), or 0 the reference's two */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
 

@@ -139,3 +139,27 @@ def test_graph_follows_projector_option(prob):
     u.set_option(7, 0)
     ref0, _ = u.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
     assert torch.equal(tv0, ref0)
+
+
+def test_merged_residual_matches_reference_order(prob):
+    """ACU_OPT_RESIDUAL: the initial CG residual from one backprojection of
+    fk - radon(uk) (default) against the reference's mu*iradon(fk) -
+    mu*iradon(radon(uk)); both within the bar of the FP64 oracle and close to
+    each other (the same operators, evaluated in another order)."""
+    a = prob["args"]
+    f = torch.from_numpy(prob["f"][:4]).cuda()
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    assert t.get_option(9) == 1
+    tv1, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    t.set_option(9, 0)
+    tv0, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    assert not torch.equal(tv0, tv1)
+    for tv in (tv0, tv1):
+        assert rel(tv, prob["tv64"][:4], prob["mask"]) < TV_TOL
+    assert rel(tv1, tv0, prob["mask"]) < 2e-5
+    # two inner iterations take the same path
+    t.set_option(9, 1)
+    tv2, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
+    t.set_option(9, 0)
+    tv3, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
+    assert rel(tv2, tv3, prob["mask"]) < 2e-5
