@@ -373,17 +373,18 @@ __device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, cons
 // the row advanced the shared row is reused and two taps are loaded; any
 // other move loads all four.  Values and summation order are those of
 // radon_stag_ray<V, EX, false>, so the results are identical.
-template <int V, bool EX, int DIR>
-__device__ __forceinline__ void radon_stag_ray_reuse(const float* __restrict__ base, int N, int kb, int kmin,
-                                                     int kmax, const ProjRay<float, EX>& ray, float mid, int jy,
-                                                     bool transposed, float (&acc)[V])
+template <int V, bool EX, int DIR, bool TR>
+__device__ __forceinline__ void radon_stag_ray_reuse(const float* __restrict__ base, int N, int kb, int i0, int i1,
+                                                     const ProjRay<float, EX>& ray, float mid, int jy,
+                                                     float (&acc)[V])
 {
+    constexpr bool transposed = TR;
     int pr = -4, pc = -4;          // cell of the taps held (none yet)
     Lanes<float, V> a, b, cc, d;   // (pr,pc) (pr,pc+1) (pr+1,pc) (pr+1,pc+1)
 #pragma unroll
     for (int v = 0; v < V; ++v) a.v[v] = b.v[v] = cc.v[v] = d.v[v] = 0.f;
     const size_t NV = (size_t)N * V;
-    for (int i = 1 + kmin; i <= N + kmax; ++i) {
+    for (int i = i0; i <= i1; ++i) {
         const int jx = i - kb;
         if (jx < 1 || jx > N || jy > N) continue;
         int x1, y1;
@@ -432,12 +433,32 @@ __device__ __forceinline__ void radon_stag_ray_reuse(const float* __restrict__ b
     }
 }
 
+// Steps jx of one ray (bin offset dy = jy - m) whose sample can lie in a
+// valid cell, 2 <= xr < N and 2 <= yr < N, from the real-valued line
+// (tomography/tv_hpc.F90:144-149) with a margin of two steps; a coordinate
+// that hardly moves along the ray (|cos| or |sin| < 1e-3) is left
+// unconstrained.  lo > hi: none.
+__device__ __forceinline__ void valid_steps(float s, float c, float dy, float mid, int N, int& lo, int& hi)
+{
+    float a = -1e30f, b = 1e30f;   // bounds on jx - m
+    auto axis = [&](float slope, float off) {
+        if (fabsf(slope) < 1e-3f) return;
+        const float t0 = (2.f - off) / slope, t1 = ((float)N - off) / slope;
+        a = fmaxf(a, fminf(t0, t1));
+        b = fminf(b, fmaxf(t0, t1));
+    };
+    axis(c, mid - s * dy);   // xr = c (jx - m) - s dy + m
+    axis(s, mid + c * dy);   // yr = s (jx - m) + c dy + m
+    lo = max(1, (int)floorf(fmaxf(a + mid, -1e8f)) - 2);
+    hi = min(N, (int)ceilf(fminf(b + mid, 1e8f)) + 2);
+}
+
 template <int V, bool EX>
 __global__ void __launch_bounds__(128) k_radon_stag_reuse(const float* __restrict__ I, const float* __restrict__ IT,
                                                           const float* __restrict__ sc,
                                                           const float4* __restrict__ xsc,
                                                           const int* __restrict__ order, float* __restrict__ sino,
-                                                          int N, int T, float mid)
+                                                          int N, int T, float mid, bool clip)
 {
     const int lane = threadIdx.x & 31;
     const int jy = blockIdx.x * 128 + threadIdx.y * 32 + lane + 1;
@@ -454,11 +475,29 @@ __global__ void __launch_bounds__(128) k_radon_stag_reuse(const float* __restric
     float acc[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) acc[v] = 0.f;
+    // Steps of the warp: the union of its rays' steps that can meet a valid
+    // cell (2 <= xr, yr < N), with a margin of two steps; every sample is
+    // still tested, so the range only skips samples that fail the test.
+    int i0 = 1 + kmin, i1 = N + kmax;
+    if (clip) {
+        int lo, hi;
+        valid_steps(s, c, (float)jy - mid, mid, N, lo, hi);
+        if (jy > N || lo > hi) {
+            lo = 0x3fffffff;
+            hi = -0x3fffffff;
+        }
+        i0 = max(i0, __reduce_min_sync(0xffffffffu, lo + kb));
+        i1 = min(i1, __reduce_max_sync(0xffffffffu, hi + kb));
+    }
     // the copy's rows follow y (step sin) in the image, x (step cos) in the transpose
-    if ((transposed ? c : s) >= 0.f)
-        radon_stag_ray_reuse<V, EX, 1>(base, N, kb, kmin, kmax, ray, mid, jy, transposed, acc);
-    else
-        radon_stag_ray_reuse<V, EX, -1>(base, N, kb, kmin, kmax, ray, mid, jy, transposed, acc);
+    const bool fwd = (transposed ? c : s) >= 0.f;
+    if (transposed) {
+        if (fwd) radon_stag_ray_reuse<V, EX, 1, true>(base, N, kb, i0, i1, ray, mid, jy, acc);
+        else radon_stag_ray_reuse<V, EX, -1, true>(base, N, kb, i0, i1, ray, mid, jy, acc);
+    } else {
+        if (fwd) radon_stag_ray_reuse<V, EX, 1, false>(base, N, kb, i0, i1, ray, mid, jy, acc);
+        else radon_stag_ray_reuse<V, EX, -1, false>(base, N, kb, i0, i1, ray, mid, jy, acc);
+    }
     if (jy <= N) {
         Lanes<float, V> o;
 #pragma unroll
@@ -524,16 +563,18 @@ void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, floa
 }
 
 void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st,
-                        bool par, bool reuse)
+                        bool par, bool reuse, bool clip)
 {
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
     k_make_transpose<<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, G);
     if (reuse) {
         if (g.exact)
-            k_radon_stag_reuse<4, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+            k_radon_stag_reuse<4, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid,
+                                                             clip);
         else
-            k_radon_stag_reuse<4, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
+            k_radon_stag_reuse<4, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T,
+                                                              g.mid, clip);
     } else if (par) {
         if (g.exact)
             k_radon_stag<4, true, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);
