@@ -376,9 +376,9 @@ int tv_iterate_v(acu_ctx* c, int nouter)
     const bool use_graph = c->opt_graph != 0 && !run.verbose;
     if (use_graph) {
         char key[256];
-        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
-                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, c->opt_residual, s.uk.p,
-                 s.part.p);
+        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
+                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, c->opt_residual,
+                 c->g32.d.bp_groups, s.uk.p, s.part.p);
         if (!s.graph || s.graph_key != key) {
             if (s.graph) {
                 cudaGraphExecDestroy(s.graph);
@@ -732,6 +732,11 @@ int acu_set_option(acu_ctx* c, int option, int value)
         if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_RESIDUAL must be 0 or 1");
         c->opt_residual = value;
         return ACU_OK;
+    case 10:
+        if (value != 0 && value != 1 && value != 2 && value != 4)
+            return set_err(c, ACU_ERR_INVALID, "ACU_OPT_BP_GROUPS must be 0, 1, 2 or 4");
+        c->g32.d.bp_groups = value;
+        return ACU_OK;
 
     }
     return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
@@ -750,6 +755,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case 7: *value = c->opt_projector; return ACU_OK;
     case 8: *value = c->opt_positions; return ACU_OK;
     case 9: *value = c->opt_residual; return ACU_OK;
+    case 10: *value = c->g32.d.bp_groups; return ACU_OK;
     }
     return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);
 }

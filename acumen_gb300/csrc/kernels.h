@@ -27,6 +27,7 @@ struct DevGeom {
     const float4* xsc_bp = nullptr;
     const float4* xsc_fp = nullptr;
     int exact = 0;
+    int bp_groups = 0;   // slice groups per backprojection thread: 0 auto (2 where they divide), 1, 2 or 4
 };
 
 // ---- radon operators (kernels_radon.cu); arrays in lane layout ------------

@@ -17,7 +17,7 @@ namespace acu {
 // One thread per pixel and slice group; angles summed in the reference's
 // order.  Pixels whose mask is zero are written as 0 without the angle loop.
 // ---------------------------------------------------------------------------
-template <typename Real, int V>
+template <typename Real, int V, int GPT>
 __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
                                                      const Real* __restrict__ cmask,
                                                      const Real* __restrict__ sc, Real* __restrict__ img,
@@ -25,16 +25,18 @@ __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
 {
     const int jx = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int jy = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int g = blockIdx.z;
+    const int g0 = blockIdx.z * GPT;
     if (jx > N || jy > N) return;
     const size_t pix = (size_t)(jy - 1) * N + (jx - 1);
     const Real cm = cmask[pix];
-    Lanes<Real, V> acc;
+    Lanes<Real, V> acc[GPT];
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = Real(0);
+    for (int k = 0; k < GPT; ++k)
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[k].v[v] = Real(0);
     if (cm != Real(0)) {
         const Real dx = (Real)jx - mid, dy = (Real)jy - mid;
-        const Real* qg = q + (size_t)g * T * N * V;
+        const Real* qg = q + (size_t)g0 * T * N * V;
         for (int t = 0; t < T; ++t) {
             const Lanes<Real, 2> scp = ld_lanes<Real, 2>(sc + 2 * t);
             const Real s = scp.v[0], c = scp.v[1];
@@ -44,17 +46,23 @@ __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
             if (y1 > 1 && y1 < N) {
                 const Real wl = add_rn(y1f, Real(1)) - yr;
                 const Real wh = yr - y1f;
-                const Real* row = qg + ((size_t)t * N + (y1 - 1)) * V;
-                const Lanes<Real, V> a = ld_lanes<Real, V>(row);
-                const Lanes<Real, V> b = ld_lanes<Real, V>(row + V);
 #pragma unroll
-                for (int v = 0; v < V; ++v) acc.v[v] = fma(b.v[v], wh, fma(a.v[v], wl, acc.v[v]));
+                for (int k = 0; k < GPT; ++k) {
+                    const Real* row = qg + ((size_t)(k * T + t) * N + (y1 - 1)) * V;
+                    const Lanes<Real, V> a = ld_lanes<Real, V>(row);
+                    const Lanes<Real, V> b = ld_lanes<Real, V>(row + V);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[k].v[v] = fma(b.v[v], wh, fma(a.v[v], wl, acc[k].v[v]));
+                }
             }
         }
     }
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = cm * acc.v[v];
-    st_lanes<Real, V>(img + ((size_t)g * N * N + pix) * V, acc);
+    for (int k = 0; k < GPT; ++k) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[k].v[v] = cm * acc[k].v[v];
+        st_lanes<Real, V>(img + ((size_t)(g0 + k) * N * N + pix) * V, acc[k]);
+    }
 }
 
 // The same backprojection with exact sample positions (option 8): the
@@ -62,7 +70,7 @@ __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
 // tables, so its cell and fraction agree with double precision to ~1e-7 px
 // instead of the ~1e-4 px of the reference's single-precision rounding at
 // grid sides of a few thousand.  Sums, weights and order are as above.
-template <int V>
+template <int V, int GPT>
 __global__ void __launch_bounds__(256) k_backproject_exact(const float* __restrict__ q,
                                                            const float* __restrict__ cmask,
                                                            const float4* __restrict__ xsc,
@@ -70,16 +78,18 @@ __global__ void __launch_bounds__(256) k_backproject_exact(const float* __restri
 {
     const int jx = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int jy = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int g = blockIdx.z;
+    const int g0 = blockIdx.z * GPT;
     if (jx > N || jy > N) return;
     const size_t pix = (size_t)(jy - 1) * N + (jx - 1);
     const float cm = cmask[pix];
-    Lanes<float, V> acc;
+    Lanes<float, V> acc[GPT];
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = 0.f;
+    for (int k = 0; k < GPT; ++k)
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[k].v[v] = 0.f;
     if (cm != 0.f) {
         const float dx = (float)jx - mid, dy = (float)jy - mid;
-        const float* qg = q + (size_t)g * T * N * V;
+        const float* qg = q + (size_t)g0 * T * N * V;
         for (int t = 0; t < T; ++t) {
             const float4 x = __ldg(xsc + t);
             float cell, wh;
@@ -87,30 +97,51 @@ __global__ void __launch_bounds__(256) k_backproject_exact(const float* __restri
             const int y1 = (int)cell;
             if (y1 > 1 && y1 < N) {
                 const float wl = 1.f - wh;
-                const float* row = qg + ((size_t)t * N + (y1 - 1)) * V;
-                const Lanes<float, V> a = ld_lanes<float, V>(row);
-                const Lanes<float, V> b = ld_lanes<float, V>(row + V);
 #pragma unroll
-                for (int v = 0; v < V; ++v) acc.v[v] = fmaf(b.v[v], wh, fmaf(a.v[v], wl, acc.v[v]));
+                for (int k = 0; k < GPT; ++k) {
+                    const float* row = qg + ((size_t)(k * T + t) * N + (y1 - 1)) * V;
+                    const Lanes<float, V> a = ld_lanes<float, V>(row);
+                    const Lanes<float, V> b = ld_lanes<float, V>(row + V);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[k].v[v] = fmaf(b.v[v], wh, fmaf(a.v[v], wl, acc[k].v[v]));
+                }
             }
         }
     }
 #pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = cm * acc.v[v];
-    st_lanes<float, V>(img + ((size_t)g * N * N + pix) * V, acc);
+    for (int k = 0; k < GPT; ++k) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[k].v[v] = cm * acc[k].v[v];
+        st_lanes<float, V>(img + ((size_t)(g0 + k) * N * N + pix) * V, acc[k]);
+    }
+}
+
+// Slice groups per thread: the angle's table entry and the sample position
+// are read and formed once for GPT groups (a warp-uniform table load still
+// costs the data pipe 32 x its width); each group's sum is unchanged.
+template <typename Real, int V, int GPT>
+static void backproject_go(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st)
+{
+    dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G / GPT);
+    if constexpr (sizeof(Real) == 4) {
+        if (g.exact) {
+            k_backproject_exact<V, GPT><<<grd, blk, 0, st>>>(q, g.cmask, g.xsc_bp, img, g.N, g.T, g.mid);
+            return;
+        }
+    }
+    k_backproject<Real, V, GPT><<<grd, blk, 0, st>>>(q, g.cmask, g.sc_bp, img, g.N, g.T, g.mid);
 }
 
 template <typename Real, int V>
 void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st)
 {
-    dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G);
-    if constexpr (sizeof(Real) == 4) {
-        if (g.exact) {
-            k_backproject_exact<V><<<grd, blk, 0, st>>>(q, g.cmask, g.xsc_bp, img, g.N, g.T, g.mid);
-            return;
-        }
+    if constexpr (V == 4) {
+        // 2 by default: 4 needs 64 registers and measured slower (368 vs 287 ms)
+        const int want = g.bp_groups > 0 ? g.bp_groups : 2;
+        if (want >= 4 && G % 4 == 0) return backproject_go<Real, V, 4>(g, G, q, img, st);
+        if (want >= 2 && G % 2 == 0) return backproject_go<Real, V, 2>(g, G, q, img, st);
     }
-    k_backproject<Real, V><<<grd, blk, 0, st>>>(q, g.cmask, g.sc_bp, img, g.N, g.T, g.mid);
+    backproject_go<Real, V, 1>(g, G, q, img, st);
 }
 
 // ---------------------------------------------------------------------------

@@ -71,6 +71,9 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 0 the reference's arithmetic (default), 1 exact */
 #define ACU_OPT_RESIDUAL 9    /* batched TV: the initial CG residual mu*iradon(fk) - mu*iradon(radon(uk)) as
                                  1 one backprojection of fk - radon(uk) (default), or 0 the reference's two */
+#define ACU_OPT_BP_GROUPS 10  /* 4-slice groups per backprojection thread: 0 auto (2 where the groups divide,
+                                 default), 1, 2 or 4; the angle's table entry and sample position are
+                                 shared by the groups, the sums are unchanged */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
 

@@ -227,3 +227,24 @@ def test_exact_positions_projector_and_adjoint(oracle, built_lib):
     lhs = torch.sum(t.radon(xp).double() * y.double()).item()
     rhs = torch.sum(xp.double() * t.radon_adjoint(y).double()).item()
     assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
+
+
+def test_backprojection_groups_per_thread(oracle, built_lib):
+    """ACU_OPT_BP_GROUPS: one, two or four 4-slice groups per thread give
+    identical images in both position modes (the groups share only the
+    angle's table entry and position); the group count need not divide."""
+    N, T = 257, 70
+    th = syn.angles(T)
+    t = Tomography(N, th, 10)
+    for S in (16, 20):                 # 4 groups (all counts divide), 5 groups (none does)
+        q = torch.randn(S, T, N, device="cuda")
+        for ex in (0, 1):
+            t.set_option(8, ex)
+            outs = []
+            for u in (1, 2, 4, 0):
+                t.set_option(10, u)
+                outs.append(t.backproject(q))
+            assert all(torch.equal(outs[0], o) for o in outs[1:])
+            assert rel(outs[0], oracle.backproject(q.double().cpu().numpy(), th, 10, 64)) < 1e-5
+    with pytest.raises(Exception):
+        t.set_option(10, 3)
