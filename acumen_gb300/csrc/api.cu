@@ -262,8 +262,12 @@ struct TvRun {
     // One Bregman outer iteration (tv_hpc.F90:206-346).  On entry ruk holds
     // radon(uk) for the current uk, which the first inner iteration reuses.
     bool merged = true;   // initial residual with one backprojection (ACU_OPT_RESIDUAL)
-    void outer_body()
+    int refresh = 1;      // radon(uk) recomputed every refresh-th outer iteration (ACU_OPT_RADON_REFRESH)
+    // full: end with radon(uk) recomputed (always when refresh == 1);
+    // otherwise radon(uk) is carried by ruk += alpha radon(p) in the CG loop.
+    void outer_body(bool full = true)
     {
+        const bool carry = refresh != 1;
         cudaStream_t st = c->stream;
         using E = TvEw<Real, V>;
         for (int jinner = 1; jinner <= ninner; ++jinner) {
@@ -271,7 +275,7 @@ struct TvRun {
             if (merged) {
                 // mu*iradon(fk) - mu*iradon(radon(uk)) as one backprojection of
                 // the data residual fk - radon(uk) (iradon is linear)
-                if (jinner > 1) radon(B(s->uk), B(s->ruk));
+                if (jinner > 1 && !carry) radon(B(s->uk), B(s->ruk));
                 E::diff(nsino(), B(s->fk), B(s->ruk), B(s->rp), st);
                 iradon(B(s->rp), B(s->tmp));
                 E::rhs(N, G, mu, lambda, B(s->tmp), B(s->dx), B(s->bx), B(s->dy), B(s->by), B(s->rhs), st);
@@ -279,7 +283,7 @@ struct TvRun {
             } else {
                 iradon(B(s->fk), B(s->tmp));                               // ifkt
                 E::rhs(N, G, mu, lambda, B(s->tmp), B(s->dx), B(s->bx), B(s->dy), B(s->by), B(s->rhs), st);
-                if (jinner > 1) radon(B(s->uk), B(s->ruk));
+                if (jinner > 1 && !carry) radon(B(s->uk), B(s->ruk));
                 iradon(B(s->ruk), B(s->tmp));                              // iukt
                 E::resid(N, G, mu, lambda, B(s->rhs), B(s->tmp), B(s->uk), B(s->r), B(s->p), sc, st);
             }
@@ -290,6 +294,7 @@ struct TvRun {
                 E::apply(N, G, mu, lambda, B(s->tmp), B(s->p), B(s->Ap), sc, st);
                 launch_cg_finalize(1, G * V, sc, st);
                 E::update(N, G, B(s->p), B(s->Ap), B(s->uk), B(s->r), sc, st);
+                if (carry) E::sino_axpy(T, N, G, B(s->rp), B(s->ruk), sc, st);
                 launch_cg_finalize(2, G * V, sc, st);
                 E::pupdate(N, G, B(s->r), B(s->p), sc, st);
             }
@@ -297,7 +302,7 @@ struct TvRun {
                       verbose ? B(s->ukp) : nullptr, sc, st);
             if (verbose) launch_cg_finalize(3, G * V, sc, st);
         }
-        radon(B(s->uk), B(s->ruk));
+        if (full || !carry) radon(B(s->uk), B(s->ruk));
         E::fk_update(nsino(), B(s->fk), B(s->f), B(s->ruk), st);
     }
 };
@@ -313,6 +318,7 @@ TvRun<Real, V> make_run(acu_ctx* c, TvState<Real>& s)
     run.ninner = s.ninner; run.ncg = s.ncg; run.lambda = (Real)s.lambda; run.mu = (Real)s.mu;
     run.verbose = c->opt_verbose != 0;
     run.merged = c->opt_residual != 0;
+    run.refresh = c->opt_refresh;
     run.sc = TvScalars{s.rsold.template as<double>(), s.alpha.template as<double>(), s.beta.template as<double>(),
                        s.delta.template as<double>(), s.part.template as<double>(), s.nblk};
     return run;
@@ -379,35 +385,47 @@ int tv_iterate_v(acu_ctx* c, int nouter)
         snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
                  s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, c->opt_residual,
                  c->g32.d.bp_groups, s.uk.p, s.part.p);
-        if (!s.graph || s.graph_key != key) {
-            if (s.graph) {
-                cudaGraphExecDestroy(s.graph);
-                s.graph = nullptr;
-            }
+        char key2[300];
+        snprintf(key2, sizeof key2, "%s/%d", key, c->opt_refresh);
+        if (!s.graph || s.graph_key != key2) {
+            for (cudaGraphExec_t* gx : {&s.graph, &s.graph_inc})
+                if (*gx) {
+                    cudaGraphExecDestroy(*gx);
+                    *gx = nullptr;
+                }
             // Capture on the context's private stream (the legacy stream
-            // cannot be captured); the graph is then launched on `st`.
-            cudaGraph_t graph;
-            CK(c, cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal));
-            c->stream = c->own_stream;
-            run.outer_body();
-            c->stream = st;
-            cudaError_t e = cudaStreamEndCapture(c->own_stream, &graph);
-            if (e != cudaSuccess) return set_err(c, ACU_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&s.graph, graph, 0);
-            cudaGraphDestroy(graph);
-            if (e != cudaSuccess) {
-                s.graph = nullptr;
-                return set_err(c, ACU_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+            // cannot be captured); the graphs are then launched on `st`.
+            // graph: radon(uk) recomputed at the end; graph_inc: carried.
+            for (int which = 0; which < (run.refresh == 1 ? 1 : 2); ++which) {
+                cudaGraph_t graph;
+                CK(c, cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal));
+                c->stream = c->own_stream;
+                run.outer_body(which == 0);
+                c->stream = st;
+                cudaError_t e = cudaStreamEndCapture(c->own_stream, &graph);
+                if (e != cudaSuccess) return set_err(c, ACU_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+                cudaGraphExec_t* gx = which == 0 ? &s.graph : &s.graph_inc;
+                e = cudaGraphInstantiate(gx, graph, 0);
+                cudaGraphDestroy(graph);
+                if (e != cudaSuccess) {
+                    *gx = nullptr;
+                    return set_err(c, ACU_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+                }
             }
-            s.graph_key = key;
+            s.graph_key = key2;
         }
-        for (int jo = 0; jo < nouter; ++jo) CK(c, cudaGraphLaunch(s.graph, st));
+        for (int jo = 0; jo < nouter; ++jo) {
+            const int n = s.outer_done + jo + 1;
+            const bool full = run.refresh == 1 || (run.refresh > 1 && n % run.refresh == 0);
+            CK(c, cudaGraphLaunch(full ? s.graph : s.graph_inc, st));
+        }
         s.outer_done += nouter;
         return ACU_OK;
     }
     if ((int)c->last_delta.size() != S) c->last_delta.assign(S, 0.0);
     for (int k = 1; k <= nouter; ++k) {
-        run.outer_body();
+        const int n = s.outer_done + 1;
+        run.outer_body(run.refresh == 1 || (run.refresh > 1 && n % run.refresh == 0));
         CKLAUNCH(c);
         const int jo = ++s.outer_done;
         if (run.verbose && (jo % c->opt_print_every == 0 || k == nouter)) {
@@ -732,6 +750,10 @@ int acu_set_option(acu_ctx* c, int option, int value)
         if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_RESIDUAL must be 0 or 1");
         c->opt_residual = value;
         return ACU_OK;
+    case 11:
+        if (value < 0) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_RADON_REFRESH must be >= 0");
+        c->opt_refresh = value;
+        return ACU_OK;
     case 10:
         if (value != 0 && value != 1 && value != 2 && value != 4)
             return set_err(c, ACU_ERR_INVALID, "ACU_OPT_BP_GROUPS must be 0, 1, 2 or 4");
@@ -755,6 +777,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case 7: *value = c->opt_projector; return ACU_OK;
     case 8: *value = c->opt_positions; return ACU_OK;
     case 9: *value = c->opt_residual; return ACU_OK;
+    case 11: *value = c->opt_refresh; return ACU_OK;
     case 10: *value = c->g32.d.bp_groups; return ACU_OK;
     }
     return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);

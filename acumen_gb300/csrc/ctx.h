@@ -59,7 +59,8 @@ struct TvState {
     DevBuf f, fk, ruk, rp, q;                                   // T*N per slice
     DevBuf uk, ukp, dx, dy, bx, by, rhs, r, p, Ap, tmp;         // N*N per slice
     DevBuf rsold, alpha, beta, delta, part;                     // FP64 scalars
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr;       // one outer iteration (radon(uk) recomputed at its end)
+    cudaGraphExec_t graph_inc = nullptr;   // the same with radon(uk) carried by the CG updates only
     std::string graph_key;
     // the active batched problem (acu_tv_begin .. acu_tv_end)
     bool active = false;
@@ -68,6 +69,7 @@ struct TvState {
     ~TvState()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (graph_inc) cudaGraphExecDestroy(graph_inc);
     }
 };
 
@@ -84,6 +86,7 @@ struct acu_ctx {
     int opt_verbose = 0;
     int opt_print_every = 50;
     int opt_slice_base = 1;
+    int opt_refresh = 5;     // radon(uk): 1 recomputed every outer iteration (reference), K >= 2 every K-th, 0 never
     int opt_residual = 1;    // 1 initial CG residual from one backprojection of fk - radon(uk), 0 two (reference)
     int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions
     int opt_projector = 4;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 the same with

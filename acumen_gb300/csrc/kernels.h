@@ -114,6 +114,8 @@ struct TvEw {
     static void shrink(int N, int G, Real lambda, const Real* uk, Real* dx, Real* bx, Real* dy,
                        Real* by, const Real* ukp, const TvScalars& sc, cudaStream_t st);
     static void fk_update(size_t n, Real* fk, const Real* f, const Real* ruk, cudaStream_t st);
+    // y += alpha_slice * x over sinograms (radon(uk) carried through uk += alpha p)
+    static void sino_axpy(int T, int N, int G, const Real* x, Real* y, const TvScalars& sc, cudaStream_t st);
     // out = a - b (the data residual fk - radon(uk) of the merged initial residual)
     static void diff(size_t n, const Real* a, const Real* b, Real* out, cudaStream_t st);
 };

@@ -336,6 +336,33 @@ void TvEw<Real, V>::fk_update(size_t n, Real* fk, const Real* f, const Real* ruk
     size_t b = (n + 255) / 256;
     k_fk<Real><<<(unsigned)(b < 4096 ? b : 4096), 256, 0, st>>>(n, fk, f, ruk);
 }
+// radon(uk + alpha p) = radon(uk) + alpha radon(p): the projection of the
+// iterate follows the CG update without a projector launch.
+template <typename Real, int V>
+__global__ void __launch_bounds__(EW_THREADS) k_sino_axpy(size_t npos, const double* __restrict__ alpha,
+                                                          const Real* __restrict__ x, Real* __restrict__ y)
+{
+    const int g = blockIdx.y;
+    Real al[V];
+#pragma unroll
+    for (int v = 0; v < V; ++v) al[v] = (Real)alpha[g * V + v];
+    const size_t base = (size_t)g * npos * V;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npos; i += (size_t)gridDim.x * blockDim.x) {
+        const size_t ii = base + i * V;
+        Lanes<Real, V> yy = ld_lanes_rw<Real, V>(y + ii);
+        const Lanes<Real, V> xx = ld_lanes_rw<Real, V>(x + ii);
+#pragma unroll
+        for (int v = 0; v < V; ++v) yy.v[v] = yy.v[v] + al[v] * xx.v[v];
+        st_lanes<Real, V>(y + ii, yy);
+    }
+}
+template <typename Real, int V>
+void TvEw<Real, V>::sino_axpy(int T, int N, int G, const Real* x, Real* y, const TvScalars& sc, cudaStream_t st)
+{
+    dim3 grd(sc.nblk, G);
+    k_sino_axpy<Real, V><<<grd, EW_THREADS, 0, st>>>((size_t)T * N, sc.alpha, x, y);
+}
+
 template <typename Real>
 __global__ void k_diff(size_t n, const Real* __restrict__ a, const Real* __restrict__ b, Real* __restrict__ out)
 {

@@ -49,7 +49,7 @@ RADON_TRAFFIC_PER_GROUP = (307.66e6 + 37.41e6) + (67.22e6 + 17.71e6)
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=5)   # one period of the radon(uk) refresh
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--slices", type=int, default=S_BATCH)
@@ -436,10 +436,15 @@ def main():
     # finaliser kernels (100 for ninner=1, ncg=10 with the merged initial
     # residual, 101 with the reference's two backprojections)
     merged = t.get_option(9) == 1
-    n_radon = NINNER * NCG + (NINNER - 1) + 1
+    refresh = t.get_option(11)        # radon(uk) recomputed every refresh-th outer iteration
+    carried = refresh != 1
+    n_full = args.steps if not carried else (0 if refresh == 0 else sum(
+        1 for k in range(args.warmup + 1, args.warmup + args.steps + 1) if k % refresh == 0))
+    n_radon = NINNER * NCG + (0 if carried else NINNER - 1)
     n_iradon = NINNER * ((1 if merged else 2) + NCG)
     n_ew = NINNER * ((5 if merged else 4) + 5 * NCG) + 1
-    kernel_launches = 2 * n_radon + 2 * n_iradon + n_ew
+    n_ew += NINNER * NCG if carried else 0          # the sinogram updates ruk += alpha radon(p)
+    kernel_launches = (2 * n_radon + 2 * n_iradon + n_ew) * args.steps + 2 * n_full
 
     line = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True, "scaling": "weak",
@@ -451,7 +456,7 @@ def main():
                        "l2": "inputs larger than L2 (batch state > 50 GB)",
                        "positions": args.positions,
                        "t_warm_s": t_warm, "t_step_s": t_step},
-            "clocks": clocks, "gpu_launches": kernel_launches * args.steps}
+            "clocks": clocks, "gpu_launches": kernel_launches}
 
     if rank == 0 and not args.no_extras:
         # dominant kernel: the projector, timed alone on the same batch (lane layout, 64 slice groups)

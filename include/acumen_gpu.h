@@ -74,6 +74,10 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_BP_GROUPS 10  /* 4-slice groups per backprojection thread: 0 auto (2 where the groups divide,
                                  default), 1, 2 or 4; the angle's table entry and sample position are
                                  shared by the groups, the sums are unchanged */
+#define ACU_OPT_RADON_REFRESH 11 /* batched TV: radon(uk) for the Bregman update recomputed every outer
+                                 iteration (1, the reference), or carried through the CG updates
+                                 (radon(uk + a p) = radon(uk) + a radon(p)) and recomputed every K-th
+                                 outer iteration (K >= 2, default 5; 0 never) */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
 

@@ -163,3 +163,32 @@ def test_merged_residual_matches_reference_order(prob):
     t.set_option(9, 0)
     tv3, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
     assert rel(tv2, tv3, prob["mask"]) < 2e-5
+
+
+def test_carried_projection_of_the_iterate(prob):
+    """ACU_OPT_RADON_REFRESH: radon(uk) carried through the CG updates and
+    recomputed every K-th outer iteration (K = 3) or never (K = 0) stays
+    within the FP64 bar and close to the recomputed form; the captured-graph
+    schedule (two graphs) equals the launch-by-launch one."""
+    a = prob["args"]
+    f = torch.from_numpy(prob["f"][:4]).cuda()
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    assert t.get_option(11) == 5
+    t.set_option(11, 1)
+    ref, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    for k in (5, 3, 0):
+        t.set_option(11, k)
+        tv, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+        assert rel(tv, prob["tv64"][:4], prob["mask"]) < TV_TOL
+        assert rel(tv, ref, prob["mask"]) < 2e-5
+    t.set_option(11, 3)
+    tv_g, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    t.set_option(3, 0)
+    tv_l, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    torch.testing.assert_close(tv_g, tv_l, rtol=0, atol=0)
+    # two inner iterations carry it too
+    t.set_option(3, 1)
+    tv2, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
+    t.set_option(11, 1)
+    tv1, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
+    assert rel(tv2, tv1, prob["mask"]) < 2e-5
