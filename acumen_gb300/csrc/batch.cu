@@ -318,7 +318,8 @@ __global__ void k_batch_resid(const ProbDesc* pd, int nprob, float mu, float lam
     for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const int x = (int)(i % N), y = (int)(i / N);
         const size_t ii = d.img + i;
-        const float v = (rhs[ii] - mu * iukt[ii]) - lambda * lap5(u, N, x, y);
+        // iukt == nullptr: rhs already holds mu * iradon(fk - radon(uk))
+        const float v = (rhs[ii] - mu * (iukt ? iukt[ii] : 0.f)) - lambda * lap5(u, N, x, y);
         r[ii] = v;
         p[ii] = v;
         acc += (double)v * (double)v;
@@ -405,6 +406,22 @@ __global__ void k_batch_fk(long long n, float* fk, const float* f, const float* 
 {
     for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
         fk[i] = (fk[i] + f[i]) - ruk[i];
+}
+
+__global__ void k_batch_diff(long long n, const float* a, const float* b, float* out)
+{
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        out[i] = a[i] - b[i];
+}
+
+// ruk += alpha radon(p) over each problem's sinogram (blockIdx.y = problem)
+__global__ void k_batch_sino_axpy(const ProbDesc* pd, const double* alpha, const float* x, float* y)
+{
+    const ProbDesc d = pd[blockIdx.y];
+    const float al = (float)alpha[blockIdx.y];
+    const long long n = (long long)d.T * d.N;
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+        y[d.sino + i] = y[d.sino + i] + al * x[d.sino + i];
 }
 
 __global__ void k_batch_finalize(const ProbDesc* pd, int nprob, long long n_ew, int which, const double* part,
@@ -507,6 +524,14 @@ void batch_fk(const BatchDev& b, float* fk, const float* f, const float* ruk, cu
 {
     k_batch_fk<<<4096, 256, 0, st>>>(b.sino_total, fk, f, ruk);
 }
+void batch_diff(const BatchDev& b, const float* a, const float* c, float* out, cudaStream_t st)
+{
+    k_batch_diff<<<4096, 256, 0, st>>>(b.sino_total, a, c, out);
+}
+void batch_sino_axpy(const BatchDev& b, const double* alpha, const float* x, float* y, cudaStream_t st)
+{
+    k_batch_sino_axpy<<<dim3(64, b.nprob), 256, 0, st>>>(b.pd, alpha, x, y);
+}
 void batch_finalize(const BatchDev& b, int which, const double* part, double* rsold, double* alpha, double* beta,
                     cudaStream_t st)
 {
@@ -530,12 +555,14 @@ struct acu_batch {
     DevBuf d_pd, d_sc_bp, d_sc_fp, d_xsc_bp, d_xsc_fp, d_cm, d_fh, d_tw, d_counter;
     DevBuf f, fk, ruk, rp, q, uk, dx, dy, bx, by, rhs, r, p, Ap, tmp, part, rsold, alpha, beta, it_img;
     DevBuf io_in, io_out;
-    cudaGraphExec_t graph = nullptr;
+    cudaGraphExec_t graph = nullptr, graph_inc = nullptr;
     std::string graph_key;
     bool tuned = false;
+    int refresh = 5;   // radon(uk) recomputed every refresh-th outer iteration (ACU_OPT_RADON_REFRESH)
     ~acu_batch()
     {
         if (graph) cudaGraphExecDestroy(graph);
+        if (graph_inc) cudaGraphExecDestroy(graph_inc);
         if (ctx) acu_ctx_destroy(ctx);
     }
 };
@@ -551,8 +578,12 @@ int berr(acu_batch* b, int code, const char* msg)
 
 // One Bregman outer iteration of every problem (tv_hpc.F90:205-353), ruk =
 // radon(uk) on entry.
-void batch_outer(acu_batch* b, cudaStream_t st, int ninner, int ncg, float lambda, float mu)
+// One outer iteration, with the uniform solver's two restructurings: the
+// initial residual from one backprojection of fk - radon(uk), and radon(uk)
+// carried through the CG updates unless `full` (or refresh == 1).
+void batch_outer(acu_batch* b, cudaStream_t st, int ninner, int ncg, float lambda, float mu, bool full)
 {
+    const bool carry = b->refresh != 1;
     const BatchDev& d = b->dev;
     auto F = [](DevBuf& x) { return x.as<float>(); };
     auto D = [](DevBuf& x) { return x.as<double>(); };
@@ -561,11 +592,11 @@ void batch_outer(acu_batch* b, cudaStream_t st, int ninner, int ncg, float lambd
         batch_backproject(d, F(b->q), img, 1, st);
     };
     for (int ji = 1; ji <= ninner; ++ji) {
-        iradon(F(b->fk), F(b->tmp));
+        if (ji > 1 && !carry) batch_radon(d, F(b->uk), F(b->ruk), 0, st);
+        batch_diff(d, F(b->fk), F(b->ruk), F(b->rp), st);
+        iradon(F(b->rp), F(b->tmp));
         batch_rhs(d, mu, lambda, F(b->tmp), F(b->dx), F(b->bx), F(b->dy), F(b->by), F(b->rhs), st);
-        if (ji > 1) batch_radon(d, F(b->uk), F(b->ruk), 0, st);
-        iradon(F(b->ruk), F(b->tmp));
-        batch_resid(d, mu, lambda, F(b->rhs), F(b->tmp), F(b->uk), F(b->r), F(b->p), D(b->part), st);
+        batch_resid(d, mu, lambda, F(b->rhs), nullptr, F(b->uk), F(b->r), F(b->p), D(b->part), st);
         batch_finalize(d, 0, D(b->part), D(b->rsold), D(b->alpha), D(b->beta), st);
         for (int k = 0; k < ncg; ++k) {
             batch_radon(d, F(b->p), F(b->rp), 0, st);
@@ -573,12 +604,13 @@ void batch_outer(acu_batch* b, cudaStream_t st, int ninner, int ncg, float lambd
             batch_apply(d, mu, lambda, F(b->tmp), F(b->p), F(b->Ap), D(b->part), st);
             batch_finalize(d, 1, D(b->part), D(b->rsold), D(b->alpha), D(b->beta), st);
             batch_update(d, F(b->p), F(b->Ap), F(b->uk), F(b->r), D(b->alpha), D(b->part), st);
+            if (carry) batch_sino_axpy(d, D(b->alpha), F(b->rp), F(b->ruk), st);
             batch_finalize(d, 2, D(b->part), D(b->rsold), D(b->alpha), D(b->beta), st);
             batch_pupdate(d, F(b->r), F(b->p), D(b->beta), st);
         }
         batch_shrink(d, lambda, F(b->uk), F(b->dx), F(b->bx), F(b->dy), F(b->by), st);
     }
-    batch_radon(d, F(b->uk), F(b->ruk), 0, st);
+    if (full || !carry) batch_radon(d, F(b->uk), F(b->ruk), 0, st);
     batch_fk(d, F(b->fk), F(b->f), F(b->ruk), st);
 }
 
@@ -856,27 +888,36 @@ int batch_solve(acu_batch* b, const float* d_f_exec, int ninner, int nouter, int
     CKLAUNCH(c);
     if (nouter > 0) {
         char key[160];
-        snprintf(key, sizeof key, "%d/%d/%.9g/%.9g/%d/%d/%d", ninner, ncg, (double)lambda, (double)mu, d.radon_warps,
-                 d.bp_rows, d.exact);
+        snprintf(key, sizeof key, "%d/%d/%.9g/%.9g/%d/%d/%d/%d", ninner, ncg, (double)lambda, (double)mu,
+                 d.radon_warps, d.bp_rows, d.exact, b->refresh);
         if (!b->graph || b->graph_key != key) {
-            if (b->graph) {
-                cudaGraphExecDestroy(b->graph);
-                b->graph = nullptr;
-            }
-            cudaGraph_t g;
-            CK(c, cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal));
-            batch_outer(b, c->own_stream, ninner, ncg, lambda, mu);
-            cudaError_t e = cudaStreamEndCapture(c->own_stream, &g);
-            if (e != cudaSuccess) return set_err(c, ACU_ERR_CUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&b->graph, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) {
-                b->graph = nullptr;
-                return set_err(c, ACU_ERR_CUDA, "batch graph instantiate failed: %s", cudaGetErrorString(e));
+            for (cudaGraphExec_t* gx : {&b->graph, &b->graph_inc})
+                if (*gx) {
+                    cudaGraphExecDestroy(*gx);
+                    *gx = nullptr;
+                }
+            // graph: radon(uk) recomputed at the end; graph_inc: carried
+            for (int which = 0; which < (b->refresh == 1 ? 1 : 2); ++which) {
+                cudaGraph_t g;
+                CK(c, cudaStreamBeginCapture(c->own_stream, cudaStreamCaptureModeThreadLocal));
+                batch_outer(b, c->own_stream, ninner, ncg, lambda, mu, which == 0);
+                cudaError_t e = cudaStreamEndCapture(c->own_stream, &g);
+                if (e != cudaSuccess)
+                    return set_err(c, ACU_ERR_CUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
+                cudaGraphExec_t* gx = which == 0 ? &b->graph : &b->graph_inc;
+                e = cudaGraphInstantiate(gx, g, 0);
+                cudaGraphDestroy(g);
+                if (e != cudaSuccess) {
+                    *gx = nullptr;
+                    return set_err(c, ACU_ERR_CUDA, "batch graph instantiate failed: %s", cudaGetErrorString(e));
+                }
             }
             b->graph_key = key;
         }
-        for (int k = 0; k < nouter; ++k) CK(c, cudaGraphLaunch(b->graph, st));
+        for (int k = 1; k <= nouter; ++k) {
+            const bool full = b->refresh == 1 || (b->refresh > 1 && k % b->refresh == 0);
+            CK(c, cudaGraphLaunch(full ? b->graph : b->graph_inc, st));
+        }
     }
     CK(c, cudaMemcpyAsync(d_tv_exec, b->uk.p, sizeof(float) * d.img_total, cudaMemcpyDeviceToDevice, st));
     return ACU_OK;
@@ -946,7 +987,13 @@ int acu_batch_tuning(const acu_batch* b, int* radon_warps, int* bp_rows)
 int acu_batch_set_option(acu_batch* b, int option, int value)
 {
     if (!b) return set_err(nullptr, ACU_ERR_INVALID, "null batch");
-    if (option != ACU_OPT_POSITIONS) return berr(b, ACU_ERR_INVALID, "acu_batch_set_option: only ACU_OPT_POSITIONS");
+    if (option == ACU_OPT_RADON_REFRESH) {
+        if (value < 0) return berr(b, ACU_ERR_INVALID, "ACU_OPT_RADON_REFRESH must be >= 0");
+        b->refresh = value;
+        return ACU_OK;
+    }
+    if (option != ACU_OPT_POSITIONS)
+        return berr(b, ACU_ERR_INVALID, "acu_batch_set_option: only ACU_OPT_POSITIONS and ACU_OPT_RADON_REFRESH");
     if (value != 0 && value != 1) return berr(b, ACU_ERR_INVALID, "ACU_OPT_POSITIONS must be 0 or 1");
     b->dev.exact = value;
     return ACU_OK;

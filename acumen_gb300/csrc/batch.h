@@ -62,6 +62,8 @@ void batch_pupdate(const BatchDev& b, const float* r, float* p, const double* be
 void batch_shrink(const BatchDev& b, float lambda, const float* uk, float* dx, float* bx, float* dy, float* by,
                   cudaStream_t st);
 void batch_fk(const BatchDev& b, float* fk, const float* f, const float* ruk, cudaStream_t st);
+void batch_diff(const BatchDev& b, const float* a, const float* c, float* out, cudaStream_t st);
+void batch_sino_axpy(const BatchDev& b, const double* alpha, const float* x, float* y, cudaStream_t st);
 // which: 0 rsold = sum; 1 alpha = rsold / sum; 2 beta = sum / rsold, rsold = sum
 void batch_finalize(const BatchDev& b, int which, const double* part, double* rsold, double* alpha, double* beta,
                     cudaStream_t st);

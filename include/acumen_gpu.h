@@ -244,8 +244,10 @@ int acu_batch_tvopt(acu_batch *batch, const float *f, int ninner, int nouter, in
                     float *tv_out, float *fbp_out);
 int acu_batch_op(acu_batch *batch, int op, const float *in, float *out);
 int acu_batch_tuning(const acu_batch *batch, int *radon_warps, int *bp_rows);
-/* ACU_OPT_POSITIONS (0 or 1) for every problem of the batch; other options
- * are rejected with ACU_ERR_INVALID. */
+/* ACU_OPT_POSITIONS (0 or 1) and ACU_OPT_RADON_REFRESH (default 5) for every
+ * problem of the batch; other options are rejected with ACU_ERR_INVALID.  The
+ * batch always forms the initial CG residual from one backprojection of
+ * fk - radon(uk) (ACU_OPT_RESIDUAL = 1). */
 int acu_batch_set_option(acu_batch *batch, int option, int value);
 
 /* ---- cross-correlation registration without device allocation --------------

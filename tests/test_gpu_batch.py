@@ -82,3 +82,24 @@ def test_batch_exact_positions(probs, oracle):
         ref_tv, _ = oracle.tvopt(s, th, probs["wpu"], 1, 4, 4, 0.05, 1.0, prec=64)
         mask = oracle.cmask(N, len(th), probs["wpu"], 64) > 0
         assert rel(tv[i], ref_tv, mask) < 1e-4, i
+
+
+def test_batch_radon_refresh(probs, oracle):
+    """ACU_OPT_RADON_REFRESH on a ragged batch: radon(uk) carried through the
+    CG updates (default, recomputed every fifth outer iteration) against the
+    reference's recomputation every outer iteration."""
+    args = (probs["sinos"], 1, 6, 4, 0.05, 1.0)
+    b = RaggedBatch(probs["N"], probs["th"], probs["wpu"])
+    tv5, _ = b.tvopt(*args)
+    b.set_option(11, 1)
+    tv1, _ = b.tvopt(*args)
+    b.set_option(11, 0)
+    tv0, _ = b.tvopt(*args)
+    for i, (s, th, N) in enumerate(zip(probs["sinos"], probs["th"], probs["N"])):
+        mask = oracle.cmask(N, len(th), probs["wpu"], 64) > 0
+        ref_tv, _ = oracle.tvopt(s, th, probs["wpu"], 1, 6, 4, 0.05, 1.0, prec=64)
+        for tv in (tv5, tv1, tv0):
+            assert rel(tv[i], ref_tv, mask) < 1e-4, i
+        assert rel(tv5[i], tv1[i], mask) < 2e-5, i
+    with pytest.raises(Exception):
+        b.set_option(11, -1)
