@@ -514,7 +514,7 @@ def main():
         gb = N * N * T * S / cuda_time(lambda: t.iradon(f), 2) / 1e9
         line["fbp_gups"] = {"config1_single_slice": g1, "batch_2049sq_1200_x256": gb}
         # ragged batch (config 4 shape): 64 problems, grids {363,725,1449,2173,2897},
-        # 180-1500 angles; one outer iteration timed as tvopt(2) - tvopt(1)
+        # 180-1500 angles; one outer iteration timed as [tvopt(6) - tvopt(1)] / 5
         del f
         torch.cuda.empty_cache()
         line["uneven_batch"] = uneven_batch(positions=POSITIONS[args.positions])
