@@ -93,6 +93,9 @@ int ensure_geom(acu_ctx* c)
         gs.d.fp_order = gs.fp_order.template as<int>();
     }
     gs.d.xsc_bp = gs.xsc_bp.template as<float4>();
+    gs.hx_bp.resize(c->T);
+    std::memcpy(gs.hx_bp.data(), h.xsc_bp.data(), sizeof(float4) * c->T);
+    gs.d.h_xsc_bp = gs.hx_bp.data();
     gs.d.xsc_fp = gs.xsc_fp.template as<float4>();
     gs.d.exact = (sizeof(Real) == 4) ? c->opt_positions : 0;
     gs.d.fft_L = h.fft_L;
@@ -384,7 +387,7 @@ int tv_iterate_v(acu_ctx* c, int nouter)
         char key[256];
         snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
                  s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, c->opt_residual,
-                 c->g32.d.bp_groups, s.uk.p, s.part.p);
+                 c->g32.d.bp_groups * 10 + c->g32.d.bp_param, s.uk.p, s.part.p);
         char key2[300];
         snprintf(key2, sizeof key2, "%s/%d", key, c->opt_refresh);
         if (!s.graph || s.graph_key != key2) {
@@ -759,6 +762,10 @@ int acu_set_option(acu_ctx* c, int option, int value)
             return set_err(c, ACU_ERR_INVALID, "ACU_OPT_BP_GROUPS must be 0, 1, 2 or 4");
         c->g32.d.bp_groups = value;
         return ACU_OK;
+    case 12:
+        if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_BP_PARAM_TABLE must be 0 or 1");
+        c->g32.d.bp_param = value;
+        return ACU_OK;
 
     }
     return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
@@ -779,6 +786,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case 9: *value = c->opt_residual; return ACU_OK;
     case 11: *value = c->opt_refresh; return ACU_OK;
     case 10: *value = c->g32.d.bp_groups; return ACU_OK;
+    case 12: *value = c->g32.d.bp_param; return ACU_OK;
     }
     return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);
 }

@@ -50,6 +50,7 @@ template <typename Real>
 struct GeomSet {
     bool ready = false;
     DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_tw, fp_order, xsc_bp, xsc_fp;
+    std::vector<float4> hx_bp;   // host copy of xsc_bp
     DevGeom<Real> d;
 };
 

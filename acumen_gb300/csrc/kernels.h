@@ -6,6 +6,13 @@
 
 namespace acu {
 
+// The exact backprojection's per-angle table as a kernel parameter (up to
+// BP_TMAX angles; kernel parameters may take up to 32 KB).
+constexpr int BP_TMAX = 1920;
+struct BpTable {
+    float4 v[BP_TMAX];
+};
+
 // Geometry of one reconstruction grid on the device, for one precision.
 // All tables are computed on the host (tables.cpp) with the reference's
 // arithmetic and uploaded once.
@@ -27,6 +34,8 @@ struct DevGeom {
     const float4* xsc_bp = nullptr;
     const float4* xsc_fp = nullptr;
     int exact = 0;
+    const float4* h_xsc_bp = nullptr;   // host copy of xsc_bp (for the parameter table)
+    int bp_param = 1;                   // exact backprojection: table in the launch parameters when T <= BP_TMAX
     int bp_groups = 0;   // slice groups per backprojection thread: 0 auto (2 where they divide), 1, 2 or 4
 };
 

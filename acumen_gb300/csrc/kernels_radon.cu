@@ -7,6 +7,8 @@
 #include "common.cuh"
 #include "kernels.h"
 
+#include <cstring>
+
 namespace acu {
 
 // ---------------------------------------------------------------------------
@@ -70,11 +72,21 @@ __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
 // tables, so its cell and fraction agree with double precision to ~1e-7 px
 // instead of the ~1e-4 px of the reference's single-precision rounding at
 // grid sides of a few thousand.  Sums, weights and order are as above.
-template <int V, int GPT>
-__global__ void __launch_bounds__(256) k_backproject_exact(const float* __restrict__ q,
-                                                           const float* __restrict__ cmask,
-                                                           const float4* __restrict__ xsc,
-                                                           float* __restrict__ img, int N, int T, float mid)
+// Per-angle table reads of the exact backprojection: from global memory, or
+// from a kernel parameter (constant bank: a warp-uniform read is a constant-
+// cache broadcast and takes no L1 data-pipe wavefronts).
+struct TabGlobal {
+    const float4* p;
+    __device__ __forceinline__ float4 operator()(int t) const { return __ldg(p + t); }
+};
+struct TabParam {
+    const BpTable* p;
+    __device__ __forceinline__ float4 operator()(int t) const { return p->v[t]; }
+};
+
+template <int V, int GPT, typename Tab>
+__device__ __forceinline__ void bp_exact_body(const float* __restrict__ q, const float* __restrict__ cmask, Tab tab,
+                                              float* __restrict__ img, int N, int T, float mid)
 {
     const int jx = blockIdx.x * blockDim.x + threadIdx.x + 1;
     const int jy = blockIdx.y * blockDim.y + threadIdx.y + 1;
@@ -91,7 +103,7 @@ __global__ void __launch_bounds__(256) k_backproject_exact(const float* __restri
         const float dx = (float)jx - mid, dy = (float)jy - mid;
         const float* qg = q + (size_t)g0 * T * N * V;
         for (int t = 0; t < T; ++t) {
-            const float4 x = __ldg(xsc + t);
+            const float4 x = tab(t);
             float cell, wh;
             exact_coord(x.x, x.y, x.z, x.w, dx, dy, mid, cell, wh);
             const int y1 = (int)cell;
@@ -116,6 +128,24 @@ __global__ void __launch_bounds__(256) k_backproject_exact(const float* __restri
     }
 }
 
+template <int V, int GPT>
+__global__ void __launch_bounds__(256) k_backproject_exact(const float* __restrict__ q,
+                                                           const float* __restrict__ cmask,
+                                                           const float4* __restrict__ xsc,
+                                                           float* __restrict__ img, int N, int T, float mid)
+{
+    bp_exact_body<V, GPT>(q, cmask, TabGlobal{xsc}, img, N, T, mid);
+}
+
+template <int V, int GPT>
+__global__ void __launch_bounds__(256) k_backproject_exact_ct(const float* __restrict__ q,
+                                                              const float* __restrict__ cmask,
+                                                              const __grid_constant__ BpTable tab,
+                                                              float* __restrict__ img, int N, int T, float mid)
+{
+    bp_exact_body<V, GPT>(q, cmask, TabParam{&tab}, img, N, T, mid);
+}
+
 // Slice groups per thread: the angle's table entry and the sample position
 // are read and formed once for GPT groups (a warp-uniform table load still
 // costs the data pipe 32 x its width); each group's sum is unchanged.
@@ -125,7 +155,13 @@ static void backproject_go(const DevGeom<Real>& g, int G, const Real* q, Real* i
     dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G / GPT);
     if constexpr (sizeof(Real) == 4) {
         if (g.exact) {
-            k_backproject_exact<V, GPT><<<grd, blk, 0, st>>>(q, g.cmask, g.xsc_bp, img, g.N, g.T, g.mid);
+            if (g.bp_param && g.h_xsc_bp && g.T <= BP_TMAX) {
+                static thread_local BpTable tab;   // copied into the launch's parameters
+                std::memcpy(tab.v, g.h_xsc_bp, sizeof(float4) * g.T);
+                k_backproject_exact_ct<V, GPT><<<grd, blk, 0, st>>>(q, g.cmask, tab, img, g.N, g.T, g.mid);
+            } else {
+                k_backproject_exact<V, GPT><<<grd, blk, 0, st>>>(q, g.cmask, g.xsc_bp, img, g.N, g.T, g.mid);
+            }
             return;
         }
     }

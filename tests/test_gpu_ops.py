@@ -248,3 +248,18 @@ def test_backprojection_groups_per_thread(oracle, built_lib):
             assert rel(outs[0], oracle.backproject(q.double().cpu().numpy(), th, 10, 64)) < 1e-5
     with pytest.raises(Exception):
         t.set_option(10, 3)
+
+
+def test_backprojection_table_in_parameters(built_lib):
+    """ACU_OPT_BP_PARAM_TABLE: the exact backprojection's per-angle table read
+    from the launch parameters (T <= 1920) or from device memory gives
+    identical images; above 1920 angles the device table is used."""
+    for N, T, S in ((257, 1920, 8), (129, 1921, 8), (257, 90, 4)):
+        t = Tomography(N, syn.angles(T), 10)
+        t.set_option(8, 1)
+        assert t.get_option(12) == 1
+        q = torch.randn(S, T, N, device="cuda")
+        a = t.backproject(q)
+        t.set_option(12, 0)
+        assert torch.equal(a, t.backproject(q))
+        t.close()
