@@ -171,7 +171,8 @@ int run_op_v(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
             CK(c, c->pairPT.ensure(sizeof(float) * 8 * nimg * G));
             if (c->opt_projector >= 1)
                 launch_radon_quads(g, G, lin, c->pairPT.template as<float>(), lout, c->stream, c->opt_projector == 2,
-                                   c->opt_projector >= 3, c->opt_projector == 4);
+                                   c->opt_projector >= 3, c->opt_projector >= 4,
+                                   c->opt_projector == 5);
             else
                 launch_radon_pairs(g, G, lin, c->pairP.template as<float>(), c->pairPT.template as<float>(), lout,
                                    c->stream);
@@ -253,7 +254,8 @@ struct TvRun {
         } else if constexpr (V == 4 && sizeof(Real) == 4) {
             if (c->opt_projector >= 1)
                 launch_radon_quads(*g, G, img, c->pairPT.template as<float>(), sino, c->stream, c->opt_projector == 2,
-                                   c->opt_projector >= 3, c->opt_projector == 4);
+                                   c->opt_projector >= 3, c->opt_projector >= 4,
+                                   c->opt_projector == 5);
             else
                 launch_radon_pairs(*g, G, img, c->pairP.template as<float>(), c->pairPT.template as<float>(), sino,
                                    c->stream);
@@ -741,7 +743,7 @@ int acu_set_option(acu_ctx* c, int option, int value)
         return ACU_OK;
     case 6: c->opt_slice_base = value; return ACU_OK;
     case 7:
-        if (value < 0 || value > 4) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 to 4");
+        if (value < 0 || value > 5) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 to 5");
         c->opt_projector = value;
         return ACU_OK;
     case 8:

@@ -90,8 +90,8 @@ struct acu_ctx {
     int opt_refresh = 5;     // radon(uk): 1 recomputed every outer iteration (reference), K >= 2 every K-th, 0 never
     int opt_residual = 1;    // 1 initial CG residual from one backprojection of fk - radon(uk), 0 two (reference)
     int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions
-    int opt_projector = 4;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 the same with
-                             // row-parity loads, 3 with taps reused from the previous sample, 4 reuse + clipped steps
+    int opt_projector = 5;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 row-parity
+                             // loads, 3 taps reused, 4 reuse + clipped steps, 5 the same with paired FMAs
     std::string err;
     acu::GeomSet<float> g32;
     acu::GeomSet<double> g64;

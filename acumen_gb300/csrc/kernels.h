@@ -54,7 +54,7 @@ void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float*
 // reuse: taps of the previous sample kept in registers; clip (with reuse):
 // steps limited to those that can meet a valid cell.
 void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st,
-                        bool par = false, bool reuse = false, bool clip = false);
+                        bool par = false, bool reuse = false, bool clip = false, bool f2 = false);
 // The staggered projector for one slice per thread (plain layout); IT is a
 // work buffer of N * N floats per slice.
 void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, float* IT, float* sino, cudaStream_t st);

@@ -440,7 +440,7 @@ __device__ __forceinline__ void radon_stag_ray(const float* __restrict__ I, cons
 // the row advanced the shared row is reused and two taps are loaded; any
 // other move loads all four.  Values and summation order are those of
 // radon_stag_ray<V, EX, false>, so the results are identical.
-template <int V, bool EX, int DIR, bool TR>
+template <int V, bool EX, int DIR, bool TR, bool F2>
 __device__ __forceinline__ void radon_stag_ray_reuse(const float* __restrict__ base, int N, int kb, int i0, int i1,
                                                      const ProjRay<float, EX>& ray, float mid, int jy,
                                                      float (&acc)[V])
@@ -493,9 +493,25 @@ __device__ __forceinline__ void radon_stag_ray_reuse(const float* __restrict__ b
             pr = r0;
             pc = c0;
             const float wb = transposed ? w12 : w21, wc = transposed ? w21 : w12;
+            if constexpr (F2 && V % 2 == 0) {
+                // the same four FMAs per slice, two slices per instruction
+                const float2 W11 = make_float2(w11, w11), WB = make_float2(wb, wb);
+                const float2 WC = make_float2(wc, wc), W22 = make_float2(w22, w22);
 #pragma unroll
-            for (int v = 0; v < V; ++v)
-                acc[v] = fmaf(d.v[v], w22, fmaf(cc.v[v], wc, fmaf(b.v[v], wb, fmaf(a.v[v], w11, acc[v]))));
+                for (int v = 0; v < V; v += 2) {
+                    float2 s2 = make_float2(acc[v], acc[v + 1]);
+                    s2 = fma2(make_float2(a.v[v], a.v[v + 1]), W11, s2);
+                    s2 = fma2(make_float2(b.v[v], b.v[v + 1]), WB, s2);
+                    s2 = fma2(make_float2(cc.v[v], cc.v[v + 1]), WC, s2);
+                    s2 = fma2(make_float2(d.v[v], d.v[v + 1]), W22, s2);
+                    acc[v] = s2.x;
+                    acc[v + 1] = s2.y;
+                }
+            } else {
+#pragma unroll
+                for (int v = 0; v < V; ++v)
+                    acc[v] = fmaf(d.v[v], w22, fmaf(cc.v[v], wc, fmaf(b.v[v], wb, fmaf(a.v[v], w11, acc[v]))));
+            }
         }
     }
 }
@@ -520,7 +536,7 @@ __device__ __forceinline__ void valid_steps(float s, float c, float dy, float mi
     hi = min(N, (int)ceilf(fminf(b + mid, 1e8f)) + 2);
 }
 
-template <int V, bool EX>
+template <int V, bool EX, bool F2>
 __global__ void __launch_bounds__(128) k_radon_stag_reuse(const float* __restrict__ I, const float* __restrict__ IT,
                                                           const float* __restrict__ sc,
                                                           const float4* __restrict__ xsc,
@@ -559,11 +575,11 @@ __global__ void __launch_bounds__(128) k_radon_stag_reuse(const float* __restric
     // the copy's rows follow y (step sin) in the image, x (step cos) in the transpose
     const bool fwd = (transposed ? c : s) >= 0.f;
     if (transposed) {
-        if (fwd) radon_stag_ray_reuse<V, EX, 1, true>(base, N, kb, i0, i1, ray, mid, jy, acc);
-        else radon_stag_ray_reuse<V, EX, -1, true>(base, N, kb, i0, i1, ray, mid, jy, acc);
+        if (fwd) radon_stag_ray_reuse<V, EX, 1, true, F2>(base, N, kb, i0, i1, ray, mid, jy, acc);
+        else radon_stag_ray_reuse<V, EX, -1, true, F2>(base, N, kb, i0, i1, ray, mid, jy, acc);
     } else {
-        if (fwd) radon_stag_ray_reuse<V, EX, 1, false>(base, N, kb, i0, i1, ray, mid, jy, acc);
-        else radon_stag_ray_reuse<V, EX, -1, false>(base, N, kb, i0, i1, ray, mid, jy, acc);
+        if (fwd) radon_stag_ray_reuse<V, EX, 1, false, F2>(base, N, kb, i0, i1, ray, mid, jy, acc);
+        else radon_stag_ray_reuse<V, EX, -1, false, F2>(base, N, kb, i0, i1, ray, mid, jy, acc);
     }
     if (jy <= N) {
         Lanes<float, V> o;
@@ -630,18 +646,25 @@ void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, floa
 }
 
 void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st,
-                        bool par, bool reuse, bool clip)
+                        bool par, bool reuse, bool clip, bool f2)
 {
     dim3 bp(256), gp((g.N + 31) / 32, (g.N + 31) / 32, G);
     k_make_transpose<<<gp, bp, 0, st>>>(img, IT, g.N);
     dim3 blk(32, 4), grd((g.N + 127) / 128, g.T, G);
-    if (reuse) {
+    if (reuse && f2) {
         if (g.exact)
-            k_radon_stag_reuse<4, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid,
-                                                             clip);
+            k_radon_stag_reuse<4, true, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T,
+                                                                   g.mid, clip);
         else
-            k_radon_stag_reuse<4, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T,
-                                                              g.mid, clip);
+            k_radon_stag_reuse<4, false, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N,
+                                                                    g.T, g.mid, clip);
+    } else if (reuse) {
+        if (g.exact)
+            k_radon_stag_reuse<4, true, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N,
+                                                                    g.T, g.mid, clip);
+        else
+            k_radon_stag_reuse<4, false, false><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N,
+                                                                     g.T, g.mid, clip);
     } else if (par) {
         if (g.exact)
             k_radon_stag<4, true, true><<<grd, blk, 0, st>>>(img, IT, g.sc_fp, g.xsc_fp, g.fp_order, sino, g.N, g.T, g.mid);

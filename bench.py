@@ -468,7 +468,7 @@ def main():
         achieved = alg_bytes / t_radon / 1e9
         groups = (S + 3) // 4
         traffic = RADON_TRAFFIC_PER_GROUP * groups if (N, T) == (N_GRID, T_ANG) else None
-        line["roofline"] = {"bound": "hbm", "kernel": "k_radon_stag_reuse<4, exact> (projector, tv_hpc.F90:137-156)",
+        line["roofline"] = {"bound": "hbm", "kernel": "k_radon_stag_reuse<4, exact, f32x2> (projector, tv_hpc.F90:137-156)",
                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                             "peak_kind": kind, "traffic": traffic,
                             "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,

@@ -67,7 +67,8 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_PROJECTOR 7   /* single-precision batched projector: 0 pair images, 1 image + transpose,
                                  2 the same with the taps loaded by row parity, 3 the same with the taps
                                  of the previous sample reused, 4 reuse with each warp's steps limited
-                                 to those that can meet a valid cell (default) */
+                                 to those that can meet a valid cell, 5 the same with paired FP32 FMAs
+                                 (fma.rn.f32x2; default); 1 and 3 to 5 give identical results */
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 0 the reference's arithmetic (default), 1 exact */
 #define ACU_OPT_RESIDUAL 9    /* batched TV: the initial CG residual mu*iradon(fk) - mu*iradon(radon(uk)) as
                                  1 one backprojection of fk - radon(uk) (default), or 0 the reference's two */

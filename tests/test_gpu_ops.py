@@ -167,12 +167,12 @@ def test_projector_variants_agree(case, oracle):
     for x in (case["img"][:5].astype(np.float32), rng.standard_normal((5, case["N"], case["N"])).astype(np.float32)):
         img = torch.from_numpy(x).cuda()
         outs = []
-        for v in (0, 1, 2, 3, 4):
+        for v in (0, 1, 2, 3, 4, 5):
             t.set_option(7, v)
             outs.append(t.radon(img))
-        # reusing the previous sample's taps, and skipping steps that cannot
-        # meet a valid cell, change neither values nor order
-        assert torch.equal(outs[3], outs[1]) and torch.equal(outs[4], outs[1])
+        # reusing the previous sample's taps, skipping steps that cannot meet
+        # a valid cell and pairing the FMAs change neither values nor order
+        assert all(torch.equal(outs[v], outs[1]) for v in (3, 4, 5))
         ref = oracle.radon(x, case["th"], 32)
         for o in outs:
             assert rel(o, ref) < 1e-6
@@ -215,7 +215,7 @@ def test_exact_positions_projector_and_adjoint(oracle, built_lib):
     xc = torch.from_numpy(x).cuda()
     e_ref = rel(t.radon(xc), ref64)
     t.set_option(8, 1)
-    for proj in (4, 3, 2, 1, 0):
+    for proj in (5, 4, 3, 2, 1, 0):
         t.set_option(7, proj)
         e4 = rel(t.radon(xc), ref64)                      # batched, 4 slices per thread
         assert e4 < 3e-6 and e4 < e_ref / 5, (proj, e4, e_ref)
