@@ -96,6 +96,12 @@ int ensure_geom(acu_ctx* c)
     gs.hx_bp.resize(c->T);
     std::memcpy(gs.hx_bp.data(), h.xsc_bp.data(), sizeof(float4) * c->T);
     gs.d.h_xsc_bp = gs.hx_bp.data();
+    if (sizeof(Real) == 4) {
+        gs.hs_bp.resize(c->T);
+        for (int t = 0; t < c->T; ++t)
+            gs.hs_bp[t] = make_float4((float)h.sc_bp[2 * t], (float)h.sc_bp[2 * t + 1], 0.f, 0.f);
+        gs.d.h_sc_bp = gs.hs_bp.data();
+    }
     gs.d.xsc_fp = gs.xsc_fp.template as<float4>();
     gs.d.exact = (sizeof(Real) == 4) ? c->opt_positions : 0;
     gs.d.fft_L = h.fft_L;

@@ -67,6 +67,56 @@ __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
     }
 }
 
+// k_backproject in single precision with the per-angle (sin, cos) read from
+// the launch parameters (constant-cache broadcast; T <= BP_TMAX).
+template <int V, int GPT>
+__global__ void __launch_bounds__(256) k_backproject_ct(const float* __restrict__ q,
+                                                        const float* __restrict__ cmask,
+                                                        const __grid_constant__ BpTable tab,
+                                                        float* __restrict__ img, int N, int T, float mid)
+{
+    const int jx = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int jy = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int g0 = blockIdx.z * GPT;
+    if (jx > N || jy > N) return;
+    const size_t pix = (size_t)(jy - 1) * N + (jx - 1);
+    const float cm = cmask[pix];
+    Lanes<float, V> acc[GPT];
+#pragma unroll
+    for (int k = 0; k < GPT; ++k)
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[k].v[v] = 0.f;
+    if (cm != 0.f) {
+        const float dx = (float)jx - mid, dy = (float)jy - mid;
+        const float* qg = q + (size_t)g0 * T * N * V;
+        for (int t = 0; t < T; ++t) {
+            const float4 scp = tab.v[t];
+            const float s = scp.x, c = scp.y;
+            const float yr = add_rn(add_rn(mul_rn(s, dx), mul_rn(c, dy)), mid);
+            const float y1f = rfloor(yr);
+            const int y1 = (int)y1f;
+            if (y1 > 1 && y1 < N) {
+                const float wl = add_rn(y1f, 1.f) - yr;
+                const float wh = yr - y1f;
+#pragma unroll
+                for (int k = 0; k < GPT; ++k) {
+                    const float* row = qg + ((size_t)(k * T + t) * N + (y1 - 1)) * V;
+                    const Lanes<float, V> a = ld_lanes<float, V>(row);
+                    const Lanes<float, V> b = ld_lanes<float, V>(row + V);
+#pragma unroll
+                    for (int v = 0; v < V; ++v) acc[k].v[v] = fmaf(b.v[v], wh, fmaf(a.v[v], wl, acc[k].v[v]));
+                }
+            }
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < GPT; ++k) {
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc[k].v[v] = cm * acc[k].v[v];
+        st_lanes<float, V>(img + ((size_t)(g0 + k) * N * N + pix) * V, acc[k]);
+    }
+}
+
 // The same backprojection with exact sample positions (option 8): the
 // coordinate yr = s*dx + c*dy + mid is evaluated from the split FP64 angle
 // tables, so its cell and fraction agree with double precision to ~1e-7 px
@@ -162,6 +212,14 @@ static void backproject_go(const DevGeom<Real>& g, int G, const Real* q, Real* i
             } else {
                 k_backproject_exact<V, GPT><<<grd, blk, 0, st>>>(q, g.cmask, g.xsc_bp, img, g.N, g.T, g.mid);
             }
+            return;
+        }
+    }
+    if constexpr (sizeof(Real) == 4) {
+        if (g.bp_param && g.h_sc_bp && g.T <= BP_TMAX) {
+            static thread_local BpTable tab;   // copied into the launch's parameters
+            std::memcpy(tab.v, g.h_sc_bp, sizeof(float4) * g.T);
+            k_backproject_ct<V, GPT><<<grd, blk, 0, st>>>(q, g.cmask, tab, img, g.N, g.T, g.mid);
             return;
         }
     }

@@ -79,7 +79,7 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
                                  iteration (1, the reference), or carried through the CG updates
                                  (radon(uk + a p) = radon(uk) + a radon(p)) and recomputed every K-th
                                  outer iteration (K >= 2, default 5; 0 never) */
-#define ACU_OPT_BP_PARAM_TABLE 12 /* exact backprojection: 1 passes the per-angle table in the launch's
+#define ACU_OPT_BP_PARAM_TABLE 12 /* single-precision backprojection: 1 passes the per-angle table in the launch's
                                  parameters when T <= 1920 (constant-cache reads, default), 0 reads
                                  it from device memory; the results are identical */
 int acu_set_option(acu_ctx *ctx, int option, int value);
