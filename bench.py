@@ -40,10 +40,10 @@ N_GRID, T_ANG, S_BATCH = 2049, 1200, 256
 NINNER, NCG, NOUTER, LAM, MU, WPU = 1, 10, 50, 0.05, 1.0, 100
 POSITIONS = {"reference": 0, "exact": 1}   # ACU_OPT_POSITIONS values
 # DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one projector
-# launch (k_radon_stag_reuse<4, exact> plus its k_make_transpose) per group of
+# launch (k_radon_stag_reuse<4, exact, f32x2> plus its k_make_transpose) per group of
 # 4 slices at 2049^2 x 1200 angles, from one ncu capture of a 4-slice launch
 # (scaled by groups below)
-RADON_TRAFFIC_PER_GROUP = (307.66e6 + 37.41e6) + (67.22e6 + 17.71e6)
+RADON_TRAFFIC_PER_GROUP = (298.25e6 + 37.49e6) + (67.22e6 + 17.71e6)
 
 
 def parse():
@@ -472,8 +472,8 @@ def main():
                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                             "peak_kind": kind, "traffic": traffic,
                             "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,
-                            "note": "bound by L1 wavefronts (ncu 85 %) and issue (80 %), not by HBM (runs from "
-                                    "L2); traffic from one 4-slice ncu capture scaled by slice groups",
+                            "note": "bound by L1 data-pipe wavefronts (ncu 91 %), not by HBM (runs from L2); "
+                                    "traffic from one 4-slice ncu capture scaled by slice groups",
                             "l1_level": {"achieved_GBps": 16.0 * N * N * T * S / t_radon / 1e9,
                                          "bytes_per_sample_slice": 16,
                                          "sample_slices_per_s": N * N * T * S / t_radon}}
