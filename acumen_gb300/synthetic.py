@@ -121,7 +121,7 @@ def normalised_sinogram(ellipses, N, theta, I0, seed, flat=None, dark=0.0, mode=
     return (-torch.log(torch.clamp(counts - df, min=1e-16) / max(ob - df, 1.0))).float()
 
 
-def config1_sinogram(seed=1, device="cpu"):
+def counts_sinogram_725(seed=1, device="cpu"):
     """Plain FBP: 10 ellipses in the 512-pixel disc on the 725 grid, 720 angles
     over [0,180), Poisson counts at I0 = flat = 1e4 with dark = 100."""
     N, T = 725, 720

@@ -251,12 +251,12 @@ def accuracy(full=False):
         res["seconds"] = time.perf_counter() - t0
         return res
 
-    out = {"config2_tv": tv_case(1449, 900, 2, full)}           # single slice, 1448 bins made odd
+    out = {"tv_1449sq_900ang": tv_case(1449, 900, 2, full)}      # single slice, 1448 bins made odd
     if full:
-        out["config3_tv_one_slice"] = tv_case(N_GRID, T_ANG, 3, False)
-    # config 1: FBP of 725^2 at 720 angles
+        out["tv_2049sq_1200ang_one_slice"] = tv_case(N_GRID, T_ANG, 3, False)
+    # FBP of one 725^2 slice at 720 angles from Poisson counts
     N, T = 725, 720
-    th, ell, counts, flat, dark = syn.config1_sinogram(seed=1, device="cuda")
+    th, ell, counts, flat, dark = syn.counts_sinogram_725(seed=1, device="cuda")
     p = (-torch.log(torch.clamp(counts - dark, min=1e-16) / max(flat - dark, 1.0))).float()[None]
     t = Tomography(N, th, WPU)
     fbp64 = t.iradon(p.double())
@@ -264,13 +264,13 @@ def accuracy(full=False):
     for name, pos in POSITIONS.items():
         t.set_option(8, pos)
         res[name + "_positions_rel_l2_vs_fp64"] = rel(t.iradon(p), fbp64)
-    out["config1_fbp"] = res
+    out["fbp_725sq_720ang"] = res
     t.close()
     return out
 
 
 def pipeline(nproj=1200, ndet=2048, nrows=256, seed=3):
-    """Config 3's preprocessing: raw uint16 projections with flat/dark stacks and
+    """Preprocessing of 1200 projections of 2048 x 256: raw uint16 projections with flat/dark stacks and
     a random rotation-axis offset in [-8, 8] px -> averages, normalisation,
     0/180 picks, registration, median, resample, transpose to 256 sinograms,
     through the host-buffer C ABI (acu_proj_to_sino_u16)."""
@@ -505,15 +505,15 @@ def main():
         plain_val = 1.0 / (tp1 - t_plain_outer + NOUTER * t_plain_outer)
         line["plain_gpu"] = {"value": plain_val, "unit": "slices/s", "outer_s_per_slice": t_plain_outer,
                              "batched_over_plain": value / plain_val}
-        # FBP GUPS: config 1 single slice (725^2, 720 angles) and the batch
+        # FBP GUPS: one 725^2 slice at 720 angles, and the batch
         from acumen_gb300 import synthetic as syn
         t1c = Tomography(725, syn.angles(720), WPU)
         t1c.set_option(8, POSITIONS[args.positions])
         s1 = torch.rand(1, 720, 725, device="cuda")
         g1 = 725 * 725 * 720 / cuda_time(lambda: t1c.iradon(s1), 10) / 1e9
         gb = N * N * T * S / cuda_time(lambda: t.iradon(f), 2) / 1e9
-        line["fbp_gups"] = {"config1_single_slice": g1, "batch_2049sq_1200_x256": gb}
-        # ragged batch (config 4 shape): 64 problems, grids {363,725,1449,2173,2897},
+        line["fbp_gups"] = {"single_slice_725sq_720ang": g1, "batch_2049sq_1200_x256": gb}
+        # ragged batch: 64 problems, grids {363,725,1449,2173,2897},
         # 180-1500 angles; one outer iteration timed as [tvopt(6) - tvopt(1)] / 5
         del f
         torch.cuda.empty_cache()

@@ -1,4 +1,4 @@
-"""Ragged batches (config 4's shape, scaled down): problems of different grid
+"""Ragged batches (64-problem shape scaled down): problems of different grid
 side and angle count in one batch, each checked against the oracle.
 
 Tolerances as the uniform path: radon 1e-6, iradon 1e-5 (relative L2, FP64

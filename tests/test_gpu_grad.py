@@ -1,5 +1,4 @@
-"""Gradient of the registration-aware TV objective (config 5's differentiable
-path): the hand-written adjoint kernels against central finite differences
+"""Gradient of the registration-aware TV objective (the differentiable path): the hand-written adjoint kernels against central finite differences
 (h = 1e-3) and against the FP64 oracle gradient (oracle/acumen_oracle.c
 orc_tv_loss_grad_f64).
 
