@@ -90,5 +90,5 @@ class RaggedBatch:
         return w.value, r.value
 
     def set_option(self, option, value):
-        """acu_batch_set_option: ACU_OPT_POSITIONS (8) only."""
+        """acu_batch_set_option: ACU_OPT_POSITIONS (8) and ACU_OPT_RADON_REFRESH (11)."""
         self._check(lib().acu_batch_set_option(self._h, int(option), int(value)))
