@@ -24,18 +24,15 @@
 namespace acu {
 
 // One staggered ray of the single-slice projector (as radon_stag_ray<1> in
-// kernels_radon.cu).
-template <bool EX>
-__device__ __forceinline__ void radon_stag_ray_v1(const float* __restrict__ I, const float* __restrict__ IT, int N,
-                                                  float s, float c, const ProjRay<float, EX>& ray, float mid, int jy,
-                                                  int lane, bool transposed, float (&acc)[1])
+// kernels_radon.cu), through the image (TR = false) or its transpose, over the
+// warp's steps i0..i1.
+template <bool EX, bool TR>
+__device__ __forceinline__ void radon_stag_ray_v1(const float* __restrict__ base, int N, int kb, int i0, int i1,
+                                                  const ProjRay<float, EX>& ray, float mid, int jy,
+                                                  float (&acc)[1])
 {
-    const float ratio = transposed ? -s / c : c / s;
-    const int kb = __float2int_rn((float)lane * ratio);
-    const int kend = __float2int_rn(31.f * ratio);
-    const int kmin = min(0, kend), kmax = max(0, kend);
-    const float* base = transposed ? IT : I;
-    for (int i = 1 + kmin; i <= N + kmax; ++i) {
+    constexpr bool transposed = TR;
+    for (int i = i0; i <= i1; ++i) {
         const int jx = i - kb;
         if (jx < 1 || jx > N || jy > N) continue;
         int x1, y1;
@@ -89,8 +86,24 @@ __global__ void __launch_bounds__(512) k_batch_radon(const ProbDesc* __restrict_
         const int N = d.N;
         const float s = sc[d.sc + 2 * t], c = sc[d.sc + 2 * t + 1];
         const ProjRay<float, EX> ray(sc + d.sc, xsc + d.sc / 2, t, jy, d.mid, nullptr);
+        const bool transposed = fabsf(c) > fabsf(s);
+        const float ratio = transposed ? -s / c : c / s;
+        const int kb = __float2int_rn((float)lane * ratio);
+        const int kend = __float2int_rn(31.f * ratio);
+        // the warp's steps: those that can meet a valid cell (see valid_steps)
+        int lo, hi;
+        valid_steps(s, c, (float)jy - d.mid, d.mid, N, lo, hi);
+        if (jy > N || lo > hi) {
+            lo = 0x3fffffff;
+            hi = -0x3fffffff;
+        }
+        const int i0 = max(1 + min(0, kend), __reduce_min_sync(0xffffffffu, lo + kb));
+        const int i1 = min(N + max(0, kend), __reduce_max_sync(0xffffffffu, hi + kb));
         float acc[1] = {0.f};
-        radon_stag_ray_v1<EX>(img + d.img, IT + d.img, N, s, c, ray, d.mid, jy, lane, fabsf(c) > fabsf(s), acc);
+        if (transposed)
+            radon_stag_ray_v1<EX, true>(IT + d.img, N, kb, i0, i1, ray, d.mid, jy, acc);
+        else
+            radon_stag_ray_v1<EX, false>(img + d.img, N, kb, i0, i1, ray, d.mid, jy, acc);
         if (jy <= N) sino[d.sino + (size_t)t * N + (jy - 1)] = acc[0] / (float)N;
     }
 }

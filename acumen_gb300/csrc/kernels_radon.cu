@@ -574,25 +574,6 @@ __device__ __forceinline__ void radon_stag_ray_reuse(const float* __restrict__ b
     }
 }
 
-// Steps jx of one ray (bin offset dy = jy - m) whose sample can lie in a
-// valid cell, 2 <= xr < N and 2 <= yr < N, from the real-valued line
-// (tomography/tv_hpc.F90:144-149) with a margin of two steps; a coordinate
-// that hardly moves along the ray (|cos| or |sin| < 1e-3) is left
-// unconstrained.  lo > hi: none.
-__device__ __forceinline__ void valid_steps(float s, float c, float dy, float mid, int N, int& lo, int& hi)
-{
-    float a = -1e30f, b = 1e30f;   // bounds on jx - m
-    auto axis = [&](float slope, float off) {
-        if (fabsf(slope) < 1e-3f) return;
-        const float t0 = (2.f - off) / slope, t1 = ((float)N - off) / slope;
-        a = fmaxf(a, fminf(t0, t1));
-        b = fminf(b, fmaxf(t0, t1));
-    };
-    axis(c, mid - s * dy);   // xr = c (jx - m) - s dy + m
-    axis(s, mid + c * dy);   // yr = s (jx - m) + c dy + m
-    lo = max(1, (int)floorf(fmaxf(a + mid, -1e8f)) - 2);
-    hi = min(N, (int)ceilf(fminf(b + mid, 1e8f)) + 2);
-}
 
 template <int V, bool EX, bool F2>
 __global__ void __launch_bounds__(128) k_radon_stag_reuse(const float* __restrict__ I, const float* __restrict__ IT,

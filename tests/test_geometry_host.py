@@ -6,7 +6,7 @@ on, by emulating their float32 arithmetic in numpy (no GPU):
   2^-q (q = 23 - bits of m) and a float32 remainder; the high part of
   a*k1 + b*k2 + m is then exact in float32, and the cell and fraction agree
   with FP64 to ~1e-7 px;
-* the projector's step clipping (csrc/kernels_radon.cu valid_steps): the steps
+* the projector's step clipping (csrc/common.cuh valid_steps): the steps
   it keeps, with a two-step margin, contain every sample of the ray that
   passes the reference's validity test (tomography/tv_hpc.F90:149).
 """
@@ -68,7 +68,7 @@ def test_exact_positions_match_fp64(N):
 
 
 def valid_steps(s, c, dy, mid, N):
-    """float32 restatement of valid_steps (csrc/kernels_radon.cu)."""
+    """float32 restatement of valid_steps (csrc/common.cuh)."""
     a, b = f32(-1e30), f32(1e30)
 
     def axis(slope, off, a, b):
