@@ -230,8 +230,13 @@ template <typename Real, int V>
 void launch_backproject(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st)
 {
     if constexpr (V == 4) {
-        // 2 by default: 4 needs 64 registers and measured slower (368 vs 287 ms)
-        const int want = g.bp_groups > 0 ? g.bp_groups : 2;
+        // auto: one group when the angle table goes in the launch parameters
+        // (241 vs 255 ms exact, 236 vs 247 ms reference), else two, which
+        // share the table's data-pipe cost (287 vs 334 ms); four need 64
+        // registers and are slower in both cases
+        const bool param = sizeof(Real) == 4 && g.bp_param && g.T <= BP_TMAX &&
+                           (g.exact ? g.h_xsc_bp != nullptr : g.h_sc_bp != nullptr);
+        const int want = g.bp_groups > 0 ? g.bp_groups : (param ? 1 : 2);
         if (want >= 4 && G % 4 == 0) return backproject_go<Real, V, 4>(g, G, q, img, st);
         if (want >= 2 && G % 2 == 0) return backproject_go<Real, V, 2>(g, G, q, img, st);
     }

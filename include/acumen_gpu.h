@@ -72,9 +72,10 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 0 the reference's arithmetic (default), 1 exact */
 #define ACU_OPT_RESIDUAL 9    /* batched TV: the initial CG residual mu*iradon(fk) - mu*iradon(radon(uk)) as
                                  1 one backprojection of fk - radon(uk) (default), or 0 the reference's two */
-#define ACU_OPT_BP_GROUPS 10  /* 4-slice groups per backprojection thread: 0 auto (2 where the groups divide,
-                                 default), 1, 2 or 4; the angle's table entry and sample position are
-                                 shared by the groups, the sums are unchanged */
+#define ACU_OPT_BP_GROUPS 10  /* 4-slice groups per backprojection thread: 0 auto (default: 1 with the
+                                 angle table in the launch parameters, else 2 where the groups divide),
+                                 1, 2 or 4; the groups share the angle's table entry and sample
+                                 position, the sums are unchanged */
 #define ACU_OPT_RADON_REFRESH 11 /* batched TV: radon(uk) for the Bregman update recomputed every outer
                                  iteration (1, the reference), or carried through the CG updates
                                  (radon(uk + a p) = radon(uk) + a radon(p)) and recomputed every K-th
