@@ -2,6 +2,7 @@
 // per-slice split-Bregman TV solvers (tomography/tv_hpc.F90:1-390).
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -508,6 +509,35 @@ int tv_end(acu_ctx* c, Real* d_tv)
     return tv_end_v<Real, 1>(c, d_tv);
 }
 
+// Slices per device batch of the TV solver: all of S when they fit in the
+// device memory that is free (plus what the context already holds for the
+// solver), else the largest multiple of 4 that does, capped by
+// ACU_OPT_MAX_BATCH.  Slices are independent, so a batch solved in chunks
+// gives each slice what one batch gives it.
+template <typename Real>
+int tv_chunk(acu_ctx* c, int S, bool host_io)
+{
+    const size_t N = c->N, T = c->T;
+    // per slice: 5 sinogram-sized and 10 image-sized solver arrays, the
+    // projector's transposed copy (and pair images for variant 0), and the
+    // host-buffer entry point's device copies of f, tv and fbp
+    size_t per = sizeof(Real) * (5 * T * N + (11 + (c->opt_projector == 0 ? 2 : 0)) * N * N);
+    if (host_io) per += sizeof(float) * (T * N + 2 * N * N);
+    size_t freeb = 0, totalb = 0;
+    if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) freeb = 0;
+    TvState<Real>& st = tvstate<Real>(c);
+    size_t held = c->pairP.n + c->pairPT.n + c->w_host_in.n + c->w_host_out.n;
+    for (const DevBuf* b : {&st.f, &st.fk, &st.ruk, &st.rp, &st.q, &st.uk, &st.ukp, &st.dx, &st.dy, &st.bx, &st.by,
+                            &st.rhs, &st.r, &st.p, &st.Ap, &st.tmp})
+        held += b->n;
+    const size_t reserve = ((size_t)1 << 30) + totalb / 50;
+    const size_t avail = freeb + held > reserve ? freeb + held - reserve : 0;
+    long long smax = (long long)(avail / per);
+    if (smax >= 4) smax -= smax % 4;
+    if (c->opt_max_batch > 0) smax = std::min<long long>(smax, c->opt_max_batch);
+    return (int)std::max<long long>(1, std::min<long long>(S, smax));
+}
+
 template <typename Real>
 int tv_solve(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int ncg, Real lambda, Real mu,
              Real* d_tv, Real* d_fbp)
@@ -516,9 +546,16 @@ int tv_solve(acu_ctx* c, int S, const Real* d_f, int ninner, int nouter, int ncg
     if (S == 0) return ACU_OK;
     if (!d_f || !d_tv) return set_err(c, ACU_ERR_INVALID, "null array");
     if (nouter < 0) return set_err(c, ACU_ERR_INVALID, "iteration counts must be >= 0");
-    CKRET(tv_begin<Real>(c, S, d_f, ninner, ncg, (double)lambda, (double)mu, d_fbp));
-    CKRET(tv_iterate<Real>(c, nouter));
-    return tv_end<Real>(c, d_tv);
+    const int chunk = tv_chunk<Real>(c, S, false);
+    const size_t nsino = (size_t)c->T * c->N, nimg = (size_t)c->N * c->N;
+    for (int s0 = 0; s0 < S; s0 += chunk) {
+        const int Sc = std::min(chunk, S - s0);
+        CKRET(tv_begin<Real>(c, Sc, d_f + s0 * nsino, ninner, ncg, (double)lambda, (double)mu,
+                             d_fbp ? d_fbp + s0 * nimg : nullptr));
+        CKRET(tv_iterate<Real>(c, nouter));
+        CKRET(tv_end<Real>(c, d_tv + s0 * nimg));
+    }
+    return ACU_OK;
 }
 
 // ---- per-slice comparator: the reference's loop structure on the GPU ---------
@@ -614,19 +651,30 @@ int tv_host(acu_ctx* c, bool plain, int S, const float* f, int ninner, int noute
     CKRET(check_ctx(c, S));
     if (S == 0) return ACU_OK;
     if (!f || !tv) return set_err(c, ACU_ERR_INVALID, "null array");
-    const size_t nsino = (size_t)c->T * c->N * S, nimg = (size_t)c->N * c->N * S;
-    CK(c, c->w_host_in.ensure(sizeof(float) * nsino));
-    CK(c, c->w_host_out.ensure(sizeof(float) * nimg * (fbp ? 2 : 1)));
-    float* d_tv = c->w_host_out.template as<float>();
-    float* d_fbp = fbp ? d_tv + nimg : nullptr;
-    CK(c, cudaMemcpyAsync(c->w_host_in.p, f, sizeof(float) * nsino, cudaMemcpyHostToDevice, c->stream));
-    if (plain)
-        CKRET(tv_plain(c, S, c->w_host_in.template as<float>(), ninner, nouter, ncg, lambda, mu, d_tv, d_fbp));
-    else
-        CKRET(tv_solve<float>(c, S, c->w_host_in.template as<float>(), ninner, nouter, ncg, lambda, mu, d_tv, d_fbp));
-    CK(c, cudaMemcpyAsync(tv, d_tv, sizeof(float) * nimg, cudaMemcpyDeviceToHost, c->stream));
-    if (fbp) CK(c, cudaMemcpyAsync(fbp, d_fbp, sizeof(float) * nimg, cudaMemcpyDeviceToHost, c->stream));
-    CK(c, cudaStreamSynchronize(c->stream));
+    // chunks of slices that fit on the device (the per-slice path holds one
+    // slice at a time, so only its copies count)
+    const int chunk = plain ? std::max(1, std::min(S, c->opt_max_batch > 0 ? c->opt_max_batch : S))
+                            : tv_chunk<float>(c, S, true);
+    const size_t sino1 = (size_t)c->T * c->N, img1 = (size_t)c->N * c->N;
+    for (int s0 = 0; s0 < S; s0 += chunk) {
+        const int Sc = std::min(chunk, S - s0);
+        const size_t nsino = sino1 * Sc, nimg = img1 * Sc;
+        CK(c, c->w_host_in.ensure(sizeof(float) * nsino));
+        CK(c, c->w_host_out.ensure(sizeof(float) * nimg * (fbp ? 2 : 1)));
+        float* d_tv = c->w_host_out.template as<float>();
+        float* d_fbp = fbp ? d_tv + nimg : nullptr;
+        CK(c, cudaMemcpyAsync(c->w_host_in.p, f + s0 * sino1, sizeof(float) * nsino, cudaMemcpyHostToDevice,
+                              c->stream));
+        if (plain)
+            CKRET(tv_plain(c, Sc, c->w_host_in.template as<float>(), ninner, nouter, ncg, lambda, mu, d_tv, d_fbp));
+        else
+            CKRET(tv_solve<float>(c, Sc, c->w_host_in.template as<float>(), ninner, nouter, ncg, lambda, mu, d_tv,
+                                  d_fbp));
+        CK(c, cudaMemcpyAsync(tv + s0 * img1, d_tv, sizeof(float) * nimg, cudaMemcpyDeviceToHost, c->stream));
+        if (fbp)
+            CK(c, cudaMemcpyAsync(fbp + s0 * img1, d_fbp, sizeof(float) * nimg, cudaMemcpyDeviceToHost, c->stream));
+        CK(c, cudaStreamSynchronize(c->stream));
+    }
     return ACU_OK;
 }
 
@@ -765,6 +813,10 @@ int acu_set_option(acu_ctx* c, int option, int value)
         if (value < 0) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_RADON_REFRESH must be >= 0");
         c->opt_refresh = value;
         return ACU_OK;
+    case 13:
+        if (value < 0) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_MAX_BATCH must be >= 0");
+        c->opt_max_batch = value;
+        return ACU_OK;
     case 10:
         if (value != 0 && value != 1 && value != 2 && value != 4)
             return set_err(c, ACU_ERR_INVALID, "ACU_OPT_BP_GROUPS must be 0, 1, 2 or 4");
@@ -793,6 +845,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case 8: *value = c->opt_positions; return ACU_OK;
     case 9: *value = c->opt_residual; return ACU_OK;
     case 11: *value = c->opt_refresh; return ACU_OK;
+    case 13: *value = c->opt_max_batch; return ACU_OK;
     case 10: *value = c->g32.d.bp_groups; return ACU_OK;
     case 12: *value = c->g32.d.bp_param; return ACU_OK;
     }

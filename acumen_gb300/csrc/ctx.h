@@ -88,6 +88,7 @@ struct acu_ctx {
     int opt_verbose = 0;
     int opt_print_every = 50;
     int opt_slice_base = 1;
+    int opt_max_batch = 0;   // slices per device batch of the TV solver: 0 as many as fit
     int opt_refresh = 5;     // radon(uk): 1 recomputed every outer iteration (reference), K >= 2 every K-th, 0 never
     int opt_residual = 1;    // 1 initial CG residual from one backprojection of fk - radon(uk), 0 two (reference)
     int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions

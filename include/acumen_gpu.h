@@ -83,6 +83,10 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
 #define ACU_OPT_BP_PARAM_TABLE 12 /* single-precision backprojection: 1 passes the per-angle table in the launch's
                                  parameters when T <= 1920 (constant-cache reads, default), 0 reads
                                  it from device memory; the results are identical */
+#define ACU_OPT_MAX_BATCH 13  /* acu_tvopt / acu_tvopt_dev / acu_tvopt_plain: at most this many slices on
+                                 the device at a time (0, default: as many as fit in the free device
+                                 memory); larger calls are solved in consecutive chunks of slices, each
+                                 slice as in one batch */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
 

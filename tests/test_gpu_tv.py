@@ -192,3 +192,27 @@ def test_carried_projection_of_the_iterate(prob):
     t.set_option(11, 1)
     tv1, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
     assert rel(tv2, tv1, prob["mask"]) < 2e-5
+
+
+def test_batch_in_chunks_matches_one_batch(prob):
+    """ACU_OPT_MAX_BATCH: a call larger than the device batch is solved in
+    consecutive chunks of slices; slices are independent, so chunks of whole
+    4-slice groups give exactly the one-batch result (other chunk sizes
+    regroup the slices, which changes only the FFT's pairing of rows), both
+    through device and host buffers."""
+    a = prob["args"]
+    f = torch.from_numpy(np.concatenate([prob["f"]] * 4)[:20]).cuda()
+    args = (a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    assert t.get_option(13) == 0
+    tv_all, fbp_all = t.tvopt(f, *args)
+    t.set_option(13, 8)
+    tv8, fbp8 = t.tvopt(f, *args)
+    assert torch.equal(tv8, tv_all) and torch.equal(fbp8, fbp_all)
+    t.set_option(13, 5)
+    tv5, _ = t.tvopt(f, *args)
+    assert rel(tv5, tv_all) < 1e-5                        # regrouped: FFT row pairs differ
+    tvh, fbph = t.tvopt(f.cpu().numpy(), *args)            # host buffers, chunks of 5
+    assert rel(tvh, tv_all) < 1e-5 and rel(fbph, fbp_all) < 1e-6
+    with pytest.raises(Exception):
+        t.set_option(13, -1)
