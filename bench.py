@@ -213,6 +213,20 @@ def cpu_slices_per_s(N, T, threads=None):
 
 
 # ---------------------------------------------------------------------------
+def l1_level(achieved_gbps, clocks, **extra):
+    """The gather kernels run from L2 and L1, so their bound is the L1 data path:
+    128 bytes per clock per SM (nominal, Blackwell) x SMs x the SM clock
+    measured during the timed region.  Not a measured peak: labelled nominal."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
+    peak = 128.0 * sms * mhz * 1e6 / 1e9
+    out = {"achieved_GBps": achieved_gbps, "peak_GBps": peak, "frac": achieved_gbps / peak,
+           "peak_kind": f"nominal: 128 B/clk/SM x {sms} SMs x {mhz:.0f} MHz"}
+    out.update(extra)
+    return out
+
+
 def accuracy(full=False):
     """Errors against FP64 at the configurations' full sizes, for both
     single-precision position modes (ACU_OPT_POSITIONS).  The FP64 reference
@@ -474,9 +488,9 @@ def main():
                             "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,
                             "note": "bound by L1 data-pipe wavefronts (ncu 91 %), not by HBM (runs from L2); "
                                     "traffic from one 4-slice ncu capture scaled by slice groups",
-                            "l1_level": {"achieved_GBps": 16.0 * N * N * T * S / t_radon / 1e9,
-                                         "bytes_per_sample_slice": 16,
-                                         "sample_slices_per_s": N * N * T * S / t_radon}}
+                            "l1_level": l1_level(16.0 * N * N * T * S / t_radon / 1e9, clocks,
+                                                 bytes_per_sample_slice=16,
+                                                 sample_slices_per_s=N * N * T * S / t_radon)}
         # end to end through the host-buffer C ABI: one outer iteration with copies
         fh = f.cpu().pin_memory()
         tvh = torch.empty(S, N, N, pin_memory=True)
@@ -513,6 +527,15 @@ def main():
         g1 = 725 * 725 * 720 / cuda_time(lambda: t1c.iradon(s1), 10) / 1e9
         gb = N * N * T * S / cuda_time(lambda: t.iradon(f), 2) / 1e9
         line["fbp_gups"] = {"single_slice_725sq_720ang": g1, "batch_2049sq_1200_x256": gb}
+        # the other hot kernel: the backprojection (8 bytes per update at L1 level)
+        t_bp = cuda_time(lambda: t.backproject(f), 2)
+        line["roofline_backprojection"] = {
+            "kernel": "k_backproject_exact_ct<4, 1> (tv_hpc.F90:107-123)", "launch_ms": 1000 * t_bp,
+            "updates_per_s": N * N * T * S / t_bp,
+            "l1_level": l1_level(8.0 * N * N * T * S / t_bp / 1e9, clocks, bytes_per_update=8),
+            "note": "neighbouring pixels' taps often fall in the same bins and are broadcast within a "
+                    "quarter-warp, so bytes delivered to registers can exceed the data path's 128 B/clk; "
+                    "ncu: 77 % of L1 data-pipe wavefronts; launch includes the lane-layout conversions"}
         # ragged batch: 64 problems, grids {363,725,1449,2173,2897},
         # 180-1500 angles; one outer iteration timed as [tvopt(6) - tvopt(1)] / 5
         del f
