@@ -3,7 +3,7 @@
 // theta.dat, sinograms{k}.dat input and fbp{k}.dat / fbp_tv{k}.dat (or
 // fbp_sub / fbp_sub_tv when sub-sampling) outputs.  The MPI master/worker
 // queue over slices (:583-631) is replaced by batches of slices solved
-// together on the GPU (ACUMEN_BATCH slices per batch, default 64).
+// together on the GPU (ACUMEN_BATCH slices per batch, default 256).
 #include <chrono>
 
 #include "hpc_io.h"
@@ -40,7 +40,7 @@ int main()
             frec.emplace_back(new File(fnum(dir + (sub ? "fbp_sub" : "fbp"), k), true));
             frec_tv.emplace_back(new File(fnum(dir + (sub ? "fbp_sub_tv" : "fbp_tv"), k), true));
         }
-        const int batch = std::max(1, std::atoi((std::getenv("ACUMEN_BATCH") ? std::getenv("ACUMEN_BATCH") : "64")));
+        const int batch = std::max(1, std::atoi((std::getenv("ACUMEN_BATCH") ? std::getenv("ACUMEN_BATCH") : "256")));
         const size_t slab = (size_t)(nimagef + add) * nfiles;
         std::vector<float> sino(slab), f((size_t)batch * ntheta * nimage), tv((size_t)batch * nimage * nimage),
             fbp((size_t)batch * nimage * nimage);
