@@ -84,6 +84,7 @@ SIGNATURES = {
     "acu_proj_to_sino_u16": [P, I, I, I, P, P, I, P, I, P, I, I, P, P, P],
     "acu_xcorr_register_noalloc": [I, I, P, P, I, P, P, P, P],
     "acu_normalize_stack_u16": [P, I, I, L, P, I, P, I, P, P],
+    "acu_normalize_stack": [P, I, I, L, P, P, P, P],
     "acu_proj_to_sino": [P, I, I, I, P, P, I, P, P, P],
     "acu_tv_loss_grad_dev": [P, I, P, P, P, F, F, P, P, P],
     "acu_batch_create": [ctypes.POINTER(P), I, P, P, P, P],

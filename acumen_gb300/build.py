@@ -62,7 +62,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     return OUT
 
 
-DRIVERS = ["raw_to_hpc", "projections_to_sinogram_hpc", "fbp_hpc", "tv_hpc", "tv_hpc_slice"]
+DRIVERS = ["fits_to_hpc", "raw_to_hpc", "projections_to_sinogram_hpc", "fbp_hpc", "tv_hpc", "tv_hpc_slice"]
 BIN = os.path.join(HERE, "bin")
 
 
@@ -76,7 +76,7 @@ def build_drivers(force: bool = False) -> list:
     def one(name):
         src = os.path.join(HERE, "drivers", name + ".cpp")
         exe = os.path.join(BIN, name)
-        deps = [src, os.path.join(HERE, "drivers", "hpc_io.h"), lib]
+        deps = [src, os.path.join(HERE, "drivers", "hpc_io.h"), os.path.join(HERE, "drivers", "fits.h"), lib]
         if force or not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
             cmd = [cxx, "-O2", "-std=c++17", "-Wall", src, "-o", exe, "-L" + HERE, "-lacumen_gpu",
                    "-Wl,-rpath,$ORIGIN/.."]

@@ -317,6 +317,38 @@ int acu_normalize_stack_u16(acu_ctx* c, int mode, int nproj, long npix, const ui
     return ACU_OK;
 }
 
+int acu_normalize_stack(acu_ctx* c, int mode, int nproj, long npix, const float* raw, const float* ob,
+                        const float* df, float* out)
+{
+    CKRET(check_any(c));
+    if ((mode != 0 && mode != 1) || nproj < 0 || npix < 1 || !raw || !ob || !out || (mode == 1 && !df))
+        return set_err(c, ACU_ERR_INVALID, "invalid normalisation arguments (mode %d)", mode);
+    if (nproj == 0) return ACU_OK;
+    DevBuf d_raw, d_ob, d_df, d_out;
+    cudaStream_t st = c->stream;
+    CK(c, d_ob.ensure(sizeof(float) * npix));
+    CK(c, d_df.ensure(sizeof(float) * npix));
+    CK(c, cudaMemcpyAsync(d_ob.p, ob, sizeof(float) * npix, cudaMemcpyHostToDevice, st));
+    if (df)
+        CK(c, cudaMemcpyAsync(d_df.p, df, sizeof(float) * npix, cudaMemcpyHostToDevice, st));
+    else
+        CK(c, cudaMemsetAsync(d_df.p, 0, sizeof(float) * npix, st));
+    const long chunk = std::max<long>(1, (long)((1u << 30) / (npix * sizeof(float))));
+    const long nc = std::min<long>(chunk, nproj);
+    CK(c, d_raw.ensure(sizeof(float) * npix * nc));
+    CK(c, d_out.ensure(sizeof(float) * npix * nc));
+    for (long p0 = 0; p0 < nproj; p0 += nc) {
+        const long n = std::min<long>(nc, nproj - p0);
+        CK(c, cudaMemcpyAsync(d_raw.p, raw + (size_t)p0 * npix, sizeof(float) * npix * n, cudaMemcpyHostToDevice, st));
+        launch_normalize_f32(mode, (int)n, npix, d_raw.as<float>(), d_ob.as<float>(), d_df.as<float>(),
+                             d_out.as<float>(), st);
+        CKLAUNCH(c);
+        CK(c, cudaMemcpyAsync(out + (size_t)p0 * npix, d_out.p, sizeof(float) * npix * n, cudaMemcpyDeviceToHost, st));
+    }
+    CK(c, cudaStreamSynchronize(st));
+    return ACU_OK;
+}
+
 int acu_proj_to_sino(acu_ctx* c, int nproj, int ndet, int nrows, const float* proj, const float* theta_deg,
                      int reg_method, float* sino_out, float* theta_out, float* shift_out)
 {

@@ -224,6 +224,11 @@ int acu_proj_to_sino_dev(acu_ctx *ctx, int nproj, int ndet, int nrows, const flo
  * normalised float projections to sinograms (projections_to_sinogram_hpc.F90). */
 int acu_normalize_stack_u16(acu_ctx *ctx, int mode, int nproj, long npix, const uint16_t *raw, int nflat,
                             const uint16_t *flats, int ndark, const uint16_t *darks, float *out);
+/* The same normalisation of float projections (the pixel values cfitsio's
+ * ftgpve returns in fits_to_hpc.F90:224) given the averaged flat and dark
+ * frames (:183-210); df may be null for mode 0. */
+int acu_normalize_stack(acu_ctx *ctx, int mode, int nproj, long npix, const float *raw, const float *ob,
+                        const float *df, float *out);
 int acu_proj_to_sino(acu_ctx *ctx, int nproj, int ndet, int nrows, const float *proj, const float *theta_deg,
                      int reg_method, float *sino_out, float *theta_out, float *shift_out);
 int acu_proj_to_sino_u16(acu_ctx *ctx, int nproj, int ndet, int nrows, const uint16_t *raw,

@@ -161,3 +161,70 @@ def test_tv_hpc_slice_driver(dataset, oracle):
     fbp = np.fromfile(single / "fbp_sub_slice.dat", np.float32).reshape(N, N)
     assert rel(fbp, ref_fbp) < 1e-5
     assert rel(tv, ref_tv, oracle.cmask(N, jte - jts + 1, 4, 64) > 0) < 1e-4
+
+
+def write_fits_u16(path, img):
+    """A FITS primary array of unsigned 16-bit pixels (BITPIX 16, BZERO 32768),
+    as detector software writes them."""
+    h, w = img.shape
+    cards = [("SIMPLE", "T"), ("BITPIX", "16"), ("NAXIS", "2"), ("NAXIS1", str(w)), ("NAXIS2", str(h)),
+             ("BZERO", "32768"), ("BSCALE", "1")]
+    head = "".join(f"{k:<8}= {v:>20}".ljust(80) for k, v in cards) + "END".ljust(80)
+    head = head.ljust((len(head) + 2879) // 2880 * 2880)
+    data = (img.astype(np.int32) - 32768).astype(">i2").tobytes()
+    data += b"\0" * ((-len(data)) % 2880)
+    path.write_bytes(head.encode("ascii") + data)
+
+
+def test_fits_to_hpc_reads_the_reference_layout(dataset):
+    """fits_to_hpc on FITS images in projections/, OB/, DF/ named as the
+    reference expects (angle digits after EXP_CT_NAME): the same projections
+    as raw_to_hpc on the same counts, and theta.dat as the reference's
+    single-precision digit sum of the names (fits_to_hpc.F90:75-96)."""
+    root, exp = dataset["root"], "fits_exp"
+    base = root / exp
+    for d in ("projections", "OB", "DF", "raw"):
+        (base / d).mkdir(parents=True)
+    f32 = np.float32
+    names, th_expected = [], []
+    for j, t in enumerate(dataset["th"]):
+        m = int(round(float(t) * 1000))
+        deg, frac = m // 1000, m % 1000
+        names.append(f"{exp}_{'p' * 9}{deg:03d}_{frac:03d}_{j:04d}.fits")
+        digits = [int(c) for c in f"{deg:03d}{frac:03d}"]
+        acc = f32(0)
+        for sc, dgt in zip((100.0, 10.0, 1.0, 0.1, 0.01, 0.001), digits):
+            acc = f32(acc + f32(f32(sc) * f32(dgt)))
+        th_expected.append(acc)
+    for n, img in zip(names, dataset["proj"]):
+        write_fits_u16(base / "projections" / n, img)
+    for k, img in enumerate(dataset["flats"]):
+        write_fits_u16(base / "OB" / f"ob_{k:03d}.fits", img)
+    for k, img in enumerate(dataset["darks"]):
+        write_fits_u16(base / "DF" / f"df_{k:03d}.fits", img)
+    # the same counts through raw_to_hpc
+    raw = base / "raw"
+    dataset["proj"].tofile(raw / "projections.u16")
+    dataset["flats"].tofile(raw / "OB.u16")
+    dataset["darks"].tofile(raw / "DF.u16")
+    np.savetxt(raw / "theta.txt", np.array(th_expected, np.float32))
+    (raw / "info.txt").write_text(f"{NPROJ} {NIMG} {len(dataset['flats'])} {len(dataset['darks'])}\n")
+    env = dict(dataset["env"], EXP_CT_NAME=exp)
+    rec = base / "reconstruction"
+    for mode in ("0", "1"):
+        envm = dict(env, ACUMEN_NORM_MODE=mode)
+        run("raw_to_hpc", envm)
+        info = np.fromfile(rec / "fileinfo_projections.dat", np.float32)
+        nfs = int(info[2])
+        ref = read_split(rec, "projections", nfs, NIMG * NIMG, NPROJ)
+        out = run("fits_to_hpc", envm)
+        assert "Number of raw projections" in out and "Determining Average Background" in out
+        np.testing.assert_array_equal(np.fromfile(rec / "fileinfo_projections.dat", np.float32), info)
+        got = read_split(rec, "projections", nfs, NIMG * NIMG, NPROJ)
+        np.testing.assert_allclose(got, ref, rtol=1e-6, atol=1e-6)
+        np.testing.assert_array_equal(np.fromfile(rec / "theta.dat", np.float32), np.array(th_expected, np.float32))
+    # no open-beam images: a clear error
+    for f in (base / "OB").iterdir():
+        f.unlink()
+    r = subprocess.run([os.path.join(B.BIN, "fits_to_hpc")], env=env, capture_output=True, text=True, timeout=600)
+    assert r.returncode != 0 and "open-beam" in r.stderr
