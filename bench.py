@@ -524,7 +524,9 @@ def main():
         t1c = Tomography(725, syn.angles(720), WPU)
         t1c.set_option(8, POSITIONS[args.positions])
         s1 = torch.rand(1, 720, 725, device="cuda")
+        t1c.iradon(s1)                     # first call builds the context's tables (host)
         g1 = 725 * 725 * 720 / cuda_time(lambda: t1c.iradon(s1), 10) / 1e9
+        t.iradon(f[:4])
         gb = N * N * T * S / cuda_time(lambda: t.iradon(f), 2) / 1e9
         line["fbp_gups"] = {"single_slice_725sq_720ang": g1, "batch_2049sq_1200_x256": gb}
         # the other hot kernel: the backprojection (8 bytes per update at L1 level)
