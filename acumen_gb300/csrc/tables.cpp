@@ -105,15 +105,32 @@ void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& ou
     std::vector<double> c(L, 0.0);
     const double pid = 4.0 * std::atan(1.0);
     for (int k = -(N - 1); k <= N - 1; ++k) c[((k % L) + L) % L] = (double)out.filt[k + N];
-    // fft_h = DFT(c) / L (the inverse transform's 1/L folded in), in double
-    std::vector<double> cosj(L);
-    for (int j = 0; j < L; ++j) cosj[j] = std::cos(2.0 * pid * (double)j / (double)L);
-    out.fft_h.resize(L);
-    for (int m = 0; m < L; ++m) {
-        long double acc = c[0];
-        for (int k = 1; k < L / 2; ++k) acc += 2.0L * (long double)c[k] * (long double)cosj[((long)k * m) % L];
-        acc += (long double)c[L / 2] * ((m % 2) ? -1.0L : 1.0L);
-        out.fft_h[m] = (Real)(acc / (long double)L);
+    // fft_h = DFT(c) / L (the inverse transform's 1/L folded in), in double:
+    // an iterative radix-2 transform (L is a power of two) with every twiddle
+    // from cos/sin of its own angle; the spectrum of the symmetric kernel is
+    // real, so the (round-off) imaginary part is dropped
+    {
+        std::vector<std::complex<double>> a(L);
+        for (int k = 0; k < L; ++k) a[k] = c[k];
+        for (int i = 1, j = 0; i < L; ++i) {   // bit reversal
+            int bit = L >> 1;
+            for (; j & bit; bit >>= 1) j ^= bit;
+            j ^= bit;
+            if (i < j) std::swap(a[i], a[j]);
+        }
+        std::vector<std::complex<double>> w(L / 2);
+        for (int k = 0; k < L / 2; ++k) w[k] = std::polar(1.0, -2.0 * pid * (double)k / (double)L);
+        for (int len = 2; len <= L; len <<= 1) {
+            const int step = L / len;
+            for (int i = 0; i < L; i += len)
+                for (int k = 0; k < len / 2; ++k) {
+                    const std::complex<double> u = a[i + k], v = a[i + k + len / 2] * w[k * step];
+                    a[i + k] = u + v;
+                    a[i + k + len / 2] = u - v;
+                }
+        }
+        out.fft_h.resize(L);
+        for (int m = 0; m < L; ++m) out.fft_h[m] = (Real)(a[m].real() / (double)L);
     }
     out.fft_tw.resize(2 * (size_t)L);   // (cos, sin) of -2 pi k / L, k < L
     for (int k = 0; k < L; ++k) {
