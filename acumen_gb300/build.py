@@ -78,7 +78,7 @@ def build_drivers(force: bool = False) -> list:
         exe = os.path.join(BIN, name)
         deps = [src, os.path.join(HERE, "drivers", "hpc_io.h"), os.path.join(HERE, "drivers", "fits.h"), lib]
         if force or not os.path.exists(exe) or os.path.getmtime(exe) < max(os.path.getmtime(d) for d in deps):
-            cmd = [cxx, "-O2", "-std=c++17", "-Wall", src, "-o", exe, "-L" + HERE, "-lacumen_gpu",
+            cmd = [cxx, "-O2", "-std=c++17", "-Wall", "-pthread", src, "-o", exe, "-L" + HERE, "-lacumen_gpu",
                    "-Wl,-rpath,$ORIGIN/.."]
             r = subprocess.run(cmd, capture_output=True, text=True)
             if r.returncode != 0:

@@ -4,7 +4,9 @@
 // theta.dat and sinograms{k}.dat, and writes fbp{k}.dat.  The parameters are
 // not written back into the fileinfo (the reference's offsets 2-9 overwrite
 // clash with the 4-float layout the other programs read).  Slices are
-// reconstructed in batches of ACUMEN_BATCH (default 256) on the GPU.
+// reconstructed in batches of ACUMEN_BATCH (default 256) on the GPU, with the
+// file reads of the next batch and the writes of the previous one overlapping
+// the current batch's reconstruction (ACUMEN_PIPELINE=0: in sequence).
 #include <chrono>
 #include <memory>
 
@@ -36,22 +38,34 @@ int main()
         for (int k = 1; k <= fi.n_files_rec; ++k) frec.emplace_back(new File(fnum(dir + "fbp", k), true));
         const int batch = std::max(1, std::atoi((std::getenv("ACUMEN_BATCH") ? std::getenv("ACUMEN_BATCH") : "256")));
         const size_t slab = (size_t)nimage * nfiles;
-        std::vector<float> sino(slab), f((size_t)batch * ntheta * nimage), img((size_t)batch * nimage * nimage);
-        for (int s0 = 1; s0 <= nimagef; s0 += batch) {
-            const int B = std::min(batch, nimagef - s0 + 1);
-            for (int b = 0; b < B; ++b) {
-                const Where w = locate(s0 + b, nimagef, fi.n_files_sino);      // :383-392
-                fsino[w.file - 1]->read(w.item * (long long)slab, sino.data(), slab);
-                std::memcpy(f.data() + (size_t)b * ntheta * nimage, sino.data() + (size_t)(jts - 1) * nimage,
-                            sizeof(float) * (size_t)ntheta * nimage);
-            }
-            check(acu_iradon(ctx, B, f.data(), img.data()), ctx);             // get_slice, :394
-            for (int b = 0; b < B; ++b) {
-                const Where w = locate(s0 + b, nimagef, fi.n_files_rec);      // :396-398
-                frec[w.file - 1]->write(w.item * (long long)nimage * nimage, img.data() + (size_t)b * nimage * nimage,
-                                        (size_t)nimage * nimage);
-            }
+        // two input and two output buffers: the next batch is read and the
+        // previous one written while the GPU reconstructs the current one
+        std::vector<float> sino[2], f[2], img[2];
+        for (int k = 0; k < 2; ++k) {
+            sino[k].resize(slab);
+            f[k].resize((size_t)batch * ntheta * nimage);
+            img[k].resize((size_t)batch * nimage * nimage);
         }
+        const int nb = (nimagef + batch - 1) / batch;
+        auto count = [&](int k) { return std::min(batch, nimagef - k * batch); };
+        pipelined(
+            nb,
+            [&](int k, int slot) {
+                for (int b = 0; b < count(k); ++b) {
+                    const Where w = locate(k * batch + b + 1, nimagef, fi.n_files_sino);   // :383-392
+                    fsino[w.file - 1]->read(w.item * (long long)slab, sino[slot].data(), slab);
+                    std::memcpy(f[slot].data() + (size_t)b * ntheta * nimage,
+                                sino[slot].data() + (size_t)(jts - 1) * nimage, sizeof(float) * (size_t)ntheta * nimage);
+                }
+            },
+            [&](int k, int slot) { check(acu_iradon(ctx, count(k), f[slot].data(), img[slot].data()), ctx); },  // :394
+            [&](int k, int slot) {
+                for (int b = 0; b < count(k); ++b) {
+                    const Where w = locate(k * batch + b + 1, nimagef, fi.n_files_rec);    // :396-398
+                    frec[w.file - 1]->write(w.item * (long long)nimage * nimage,
+                                            img[slot].data() + (size_t)b * nimage * nimage, (size_t)nimage * nimage);
+                }
+            });
         acu_ctx_destroy(ctx);
         const double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         std::printf(" Total Compute time: %g\n", secs);

@@ -24,6 +24,7 @@
 #include <sstream>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/acumen_gpu.h"
@@ -194,6 +195,62 @@ inline void apply_positions(acu_ctx* ctx)
     if (v == "exact" || v == "1") check(acu_set_option(ctx, ACU_OPT_POSITIONS, 1), ctx);
     else if (!v.empty() && v != "reference" && v != "0")
         throw Fail("ACUMEN_POSITIONS must be 'reference' (0) or 'exact' (1), got '" + v + "'");
+}
+
+// Batches through read -> compute -> write with the file I/O of the next and
+// the previous batch overlapping the GPU work of the current one: read(k,
+// slot) fills input slot k % 2 on a reader thread, compute(k, slot) turns
+// input slot into output slot on the calling thread, write(k, slot) drains
+// output slot k % 2 on a writer thread.  A slot is reused only after the
+// thread that last used it has been joined.  ACUMEN_PIPELINE=0 runs the three
+// in sequence.  An exception on a worker is rethrown on the calling thread.
+template <class R, class C, class W>
+void pipelined(int nbatches, R read, C compute, W write)
+{
+    const std::string pv = env("ACUMEN_PIPELINE", false);
+    if (pv == "0") {
+        for (int k = 0; k < nbatches; ++k) {
+            read(k, 0);
+            compute(k, 0);
+            write(k, 0);
+        }
+        return;
+    }
+    std::exception_ptr err_r, err_w;
+    auto guard = [](auto fn, std::exception_ptr& e) {
+        return [fn, &e](int k, int slot) {
+            try {
+                fn(k, slot);
+            } catch (...) {
+                e = std::current_exception();
+            }
+        };
+    };
+    auto rd_fn = guard(read, err_r);
+    auto wr_fn = guard(write, err_w);
+    std::thread rd, wr;
+    auto join_all = [&]() {
+        if (rd.joinable()) rd.join();
+        if (wr.joinable()) wr.join();
+    };
+    try {
+        if (nbatches > 0) rd = std::thread(rd_fn, 0, 0);
+        for (int k = 0; k < nbatches; ++k) {
+            if (rd.joinable()) rd.join();                         // input k is in slot k % 2
+            if (err_r) std::rethrow_exception(err_r);
+            if (k + 1 < nbatches) rd = std::thread(rd_fn, k + 1, (k + 1) % 2);
+            compute(k, k % 2);                                     // output k into slot k % 2
+            if (wr.joinable()) wr.join();                          // output k - 1 written
+            if (err_w) std::rethrow_exception(err_w);
+            wr = std::thread(wr_fn, k, k % 2);
+        }
+        join_all();
+        if (err_r) std::rethrow_exception(err_r);
+        if (err_w) std::rethrow_exception(err_w);
+    } catch (...) {
+        join_all();
+        throw;
+    }
 }
 
 }  // namespace hpc

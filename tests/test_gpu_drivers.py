@@ -102,6 +102,10 @@ def test_pipeline_through_drivers(dataset, oracle):
     fbp = read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N)
     ref_fbp64 = oracle.iradon(f.astype(np.float64), tw, 4, 64)
     assert rel(fbp, ref_fbp64) < 1e-5
+    # several batches through the read / reconstruct / write pipeline, and in sequence
+    for pipe in ("1", "0"):
+        run("fbp_hpc", dict(env, ACUMEN_BATCH="10", ACUMEN_PIPELINE=pipe))
+        np.testing.assert_array_equal(read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N), fbp)
     # ACUMEN_POSITIONS=exact selects the exact sample positions; a bad value fails
     run("fbp_hpc", dict(env, ACUMEN_POSITIONS="exact"))
     fbpx = read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N)
