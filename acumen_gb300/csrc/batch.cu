@@ -459,14 +459,10 @@ __global__ void k_batch_finalize(const ProbDesc* pd, int nprob, long long n_ew, 
 // ---- launchers ---------------------------------------------------------------
 static int sm_count()
 {
-    static int n = 0;
-    if (!n) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-        if (n <= 0) n = 1;
-    }
-    return n;
+    int dev = 0, n = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);   // a cached attribute query
+    return n > 0 ? n : 1;
 }
 
 void batch_radon(const BatchDev& b, const float* img, float* sino, int slot, cudaStream_t st)
@@ -496,11 +492,7 @@ void batch_backproject(const BatchDev& b, const float* q, float* img, int slot, 
 }
 void batch_filter(const BatchDev& b, const float* sino, float* out, cudaStream_t st)
 {
-    static bool attr = false;
-    if (!attr) {
-        cudaFuncSetAttribute(k_batch_filter, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr = true;
-    }
+    max_dynamic_smem<k_batch_filter>();
     k_batch_filter<<<(unsigned)b.n_fft, 256, 2 * (size_t)b.Lmax * sizeof(float2), st>>>(b.pd, b.nprob, sino, out,
                                                                                          b.fft_h, b.tw, b.Lmax);
 }

@@ -1,5 +1,6 @@
 // Shared device helpers for the GB300 tomography kernels.
 #pragma once
+#include <atomic>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -264,6 +265,20 @@ __device__ __forceinline__ void valid_steps(float s, float c, float dy, float mi
     axis(s, mid + c * dy);   // yr = s (jx - m) + c dy + m
     lo = max(1, (int)floorf(fmaxf(a + mid, -1e8f)) - 2);
     hi = min(N, (int)ceilf(fminf(b + mid, 1e8f)) + 2);
+}
+
+// Lets kernel K use up to 227 KB of dynamic shared memory on the current
+// device (the attribute is per device; set once per device, thread-safe).
+template <auto K>
+inline void max_dynamic_smem()
+{
+    static std::atomic<unsigned long long> done{0};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (done.load(std::memory_order_acquire) & bit) return;
+    cudaFuncSetAttribute(K, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
+    done.fetch_or(bit, std::memory_order_release);
 }
 
 }  // namespace acu

@@ -150,11 +150,7 @@ void launch_filter_fft(const DevGeom<Real>& g, int G, const Real* sino, Real* ou
 {
     using C = typename Cplx<Real>::T;
     const size_t sm = 2 * (size_t)g.fft_L * sizeof(C);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_filter_fft<Real>, cudaFuncAttributeMaxDynamicSharedMemorySize, 227 * 1024);
-        attr_set = true;
-    }
+    max_dynamic_smem<k_filter_fft<Real>>();
     const C* tw = reinterpret_cast<const C*>(sizeof(Real) == 4 ? (const void*)g.fft_tw : (const void*)g.fft_tw64);
     dim3 grd(V == 4 ? 2 * g.T : (g.T + 1) / 2, G);
     k_filter_fft<Real><<<grd, 256, sm, st>>>(sino, out, g.fft_h, tw, g.N, g.T, g.fft_L, V);

@@ -861,12 +861,7 @@ void launch_filter_direct(const DevGeom<Real>& g, int G, const Real* sino, Real*
 {
     constexpr int RB = 4;
     size_t sm = sizeof(Real) * ((size_t)g.N * V + 2 * (size_t)g.N + 1 + RB);
-    static bool attr_set = false;
-    if (!attr_set) {
-        cudaFuncSetAttribute(k_filter_direct<Real, V, RB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             227 * 1024);
-        attr_set = true;
-    }
+    max_dynamic_smem<k_filter_direct<Real, V, RB>>();
     dim3 grd(g.T, G);
     k_filter_direct<Real, V, RB><<<grd, 256, sm, st>>>(sino, g.filt, out, g.N, g.T);
 }
