@@ -18,7 +18,7 @@ CSRC = os.path.join(HERE, "csrc")
 OUT = os.path.join(HERE, "libacumen_gpu.so")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-SOURCES = ["api.cu", "prep_api.cu", "kernels_radon.cu", "kernels_fft.cu", "kernels_tv.cu", "kernels_prep.cu",
+SOURCES = ["api.cu", "prep_api.cu", "kernels_radon.cu", "kernels_lines.cu", "kernels_fft.cu", "kernels_tv.cu", "kernels_prep.cu",
            "kernels_grad.cu", "batch.cu", "noalloc.cu", "tables.cpp"]
 
 

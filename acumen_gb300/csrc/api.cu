@@ -92,6 +92,17 @@ int ensure_geom(acu_ctx* c)
         CK(c, gs.fp_order.ensure(sizeof(int) * ord.size()));
         CK(c, cudaMemcpy(gs.fp_order.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
         gs.d.fp_order = gs.fp_order.template as<int>();
+        // projector variant 6: angles whose rays climb the rows (sin >= 0) first
+        ord.clear();
+        for (int pass = 0; pass < 2; ++pass)
+            for (int t = 0; t < c->T; ++t)
+                if ((h.sc_fp[2 * t] >= 0) == (pass == 0)) ord.push_back(t);
+        int nup = 0;
+        for (int t = 0; t < c->T; ++t) nup += h.sc_fp[2 * t] >= 0;
+        CK(c, gs.lines_order.ensure(sizeof(int) * ord.size()));
+        CK(c, cudaMemcpy(gs.lines_order.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
+        gs.d.lines_order = gs.lines_order.template as<int>();
+        gs.d.lines_nup = nup;
     }
     gs.d.xsc_bp = gs.xsc_bp.template as<float4>();
     gs.hx_bp.resize(c->T);
@@ -147,6 +158,47 @@ void lanes_iradon(acu_ctx* c, const DevGeom<Real>& g, int G, const Real* sino, R
 enum OpKind { OP_IRADON, OP_RADON, OP_RADON_ADJ, OP_FILTER, OP_BACKPROJECT };
 
 // Runs one operator on plain-layout device arrays of S slices.
+// The single-precision 4-slice projector variant for G slice groups:
+// ACU_OPT_PROJECTOR, where 7 (automatic) takes the pixel-line projector (6)
+// when the groups fill their 8-group lines to 8/9 or more (its cost follows
+// the lines, the others' the groups), else variant 5.
+int projector_variant(const acu_ctx* c, int G)
+{
+    if (c->opt_projector != 7) return c->opt_projector;
+    return 8 * ((G + 7) / 8) <= G + G / 8 ? 6 : 5;
+}
+
+// Work buffers of the single-precision 4-slice projector that
+// ACU_OPT_PROJECTOR selects, for G slice groups (grow-only).
+int ensure_projector_buffers(acu_ctx* c, int G)
+{
+    const size_t nimg = (size_t)c->N * c->N * G * 4;
+    const int v = projector_variant(c, G);
+    if (v == 0) {
+        CK(c, c->pairP.ensure(sizeof(float) * 2 * nimg));
+        CK(c, c->pairPT.ensure(sizeof(float) * 2 * nimg));
+    } else if (v == 6) {
+        CK(c, c->lineL.ensure(sizeof(float) * lines_image_floats(c->N, G)));
+        CK(c, c->lineA.ensure(sizeof(float) * lines_sums_floats(c->N, c->T, G)));
+    } else {
+        CK(c, c->pairPT.ensure(sizeof(float) * nimg));
+    }
+    return ACU_OK;
+}
+
+// The single-precision 4-slice projector that ACU_OPT_PROJECTOR selects
+// (buffers from ensure_projector_buffers).
+void radon_quads(acu_ctx* c, const DevGeom<float>& g, int G, const float* img, float* sino)
+{
+    const int v = projector_variant(c, G);
+    if (v == 6)
+        launch_radon_lines(g, G, img, c->lineL.as<float>(), c->lineA.as<float>(), sino, c->stream);
+    else if (v >= 1)
+        launch_radon_quads(g, G, img, c->pairPT.as<float>(), sino, c->stream, v == 2, v >= 3, v >= 4, v == 5);
+    else
+        launch_radon_pairs(g, G, img, c->pairP.as<float>(), c->pairPT.as<float>(), sino, c->stream);
+}
+
 template <typename Real, int V>
 int run_op_v(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
 {
@@ -174,15 +226,8 @@ int run_op_v(acu_ctx* c, OpKind op, int S, const Real* in, Real* out)
         break;
     case OP_RADON:
         if constexpr (V == 4 && sizeof(Real) == 4) {
-            CK(c, c->pairP.ensure(sizeof(float) * 8 * nimg * G));
-            CK(c, c->pairPT.ensure(sizeof(float) * 8 * nimg * G));
-            if (c->opt_projector >= 1)
-                launch_radon_quads(g, G, lin, c->pairPT.template as<float>(), lout, c->stream, c->opt_projector == 2,
-                                   c->opt_projector >= 3, c->opt_projector >= 4,
-                                   c->opt_projector == 5);
-            else
-                launch_radon_pairs(g, G, lin, c->pairP.template as<float>(), c->pairPT.template as<float>(), lout,
-                                   c->stream);
+            CKRET(ensure_projector_buffers(c, G));
+            radon_quads(c, g, G, lin, lout);
         } else if constexpr (V == 1 && sizeof(Real) == 4) {
             CK(c, c->pairPT.ensure(sizeof(float) * nimg * G));
             launch_radon_v1_fast(g, G, lin, c->pairPT.template as<float>(), lout, c->stream);
@@ -259,13 +304,7 @@ struct TvRun {
         if constexpr (V == 1 && sizeof(Real) == 4) {
             launch_radon_v1_fast(*g, G, img, c->pairPT.template as<float>(), sino, c->stream);
         } else if constexpr (V == 4 && sizeof(Real) == 4) {
-            if (c->opt_projector >= 1)
-                launch_radon_quads(*g, G, img, c->pairPT.template as<float>(), sino, c->stream, c->opt_projector == 2,
-                                   c->opt_projector >= 3, c->opt_projector >= 4,
-                                   c->opt_projector == 5);
-            else
-                launch_radon_pairs(*g, G, img, c->pairP.template as<float>(), c->pairPT.template as<float>(), sino,
-                                   c->stream);
+            radon_quads(c, *g, G, img, sino);
         }
         else
             launch_radon<Real, V>(*g, G, img, sino, c->stream);
@@ -351,8 +390,7 @@ int tv_begin_v(acu_ctx* c, int S, const Real* d_f, int ninner, int ncg, double l
         CK(c, b->ensure(sizeof(Real) * nimg));
     if (c->opt_verbose) CK(c, s.ukp.ensure(sizeof(Real) * nimg));
     if constexpr (V == 4 && sizeof(Real) == 4) {
-        CK(c, c->pairP.ensure(sizeof(float) * 2 * nimg));
-        CK(c, c->pairPT.ensure(sizeof(float) * 2 * nimg));
+        CKRET(ensure_projector_buffers(c, G));
     } else if constexpr (sizeof(Real) == 4) {
         CK(c, c->pairPT.ensure(sizeof(float) * nimg));
     }
@@ -392,12 +430,18 @@ int tv_iterate_v(acu_ctx* c, int nouter)
     cudaStream_t st = c->stream;
     const int S = s.S, Sp = s.G * V;
     const bool use_graph = c->opt_graph != 0 && !run.verbose;
+    // the projector option may have changed since acu_tv_begin
+    if constexpr (V == 4 && sizeof(Real) == 4) CKRET(ensure_projector_buffers(c, s.G));
     if (use_graph) {
-        char key[256];
-        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%d/%p/%p", (int)sizeof(Real), V, s.G, s.ninner,
-                 s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions, c->opt_residual,
-                 c->g32.d.bp_groups * 10 + c->g32.d.bp_param, s.uk.p, s.part.p);
-        char key2[300];
+        // the key holds every device address the captured iteration uses
+        // outside the solver state, so a work buffer that has grown since
+        // (another call on a larger batch) forces a new capture
+        char key[400];
+        snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%d/%p/%p/%p/%p/%p/%p", (int)sizeof(Real), V,
+                 s.G, s.ninner, s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions,
+                 c->opt_residual, c->g32.d.bp_groups * 10 + c->g32.d.bp_param, s.uk.p, s.part.p, c->pairP.p,
+                 c->pairPT.p, c->lineL.p, c->lineA.p);
+        char key2[440];
         snprintf(key2, sizeof key2, "%s/%d", key, c->opt_refresh);
         if (!s.graph || s.graph_key != key2) {
             for (cudaGraphExec_t* gx : {&s.graph, &s.graph_inc})
@@ -519,14 +563,17 @@ int tv_chunk(acu_ctx* c, int S, bool host_io)
 {
     const size_t N = c->N, T = c->T;
     // per slice: 5 sinogram-sized and 10 image-sized solver arrays, the
-    // projector's transposed copy (and pair images for variant 0), and the
-    // host-buffer entry point's device copies of f, tv and fbp
-    size_t per = sizeof(Real) * (5 * T * N + (11 + (c->opt_projector == 0 ? 2 : 0)) * N * N);
+    // projector's work buffers (transposed copy; pair images for variant 0;
+    // line image and ray sums for variant 6), and the host-buffer entry
+    // point's device copies of f, tv and fbp
+    const int proj = projector_variant(c, (S + 3) / 4);
+    size_t per = sizeof(Real) * (5 * T * N + 10 * N * N);
+    if (sizeof(Real) == 4) per += sizeof(float) * (proj == 0 ? 4 * N * N : proj == 6 ? N * N + T * N : N * N);
     if (host_io) per += sizeof(float) * (T * N + 2 * N * N);
     size_t freeb = 0, totalb = 0;
     if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) freeb = 0;
     TvState<Real>& st = tvstate<Real>(c);
-    size_t held = c->pairP.n + c->pairPT.n + c->w_host_in.n + c->w_host_out.n;
+    size_t held = c->pairP.n + c->pairPT.n + c->lineL.n + c->lineA.n + c->w_host_in.n + c->w_host_out.n;
     for (const DevBuf* b : {&st.f, &st.fk, &st.ruk, &st.rp, &st.q, &st.uk, &st.ukp, &st.dx, &st.dy, &st.bx, &st.by,
                             &st.rhs, &st.r, &st.p, &st.Ap, &st.tmp})
         held += b->n;
@@ -797,7 +844,7 @@ int acu_set_option(acu_ctx* c, int option, int value)
         return ACU_OK;
     case 6: c->opt_slice_base = value; return ACU_OK;
     case 7:
-        if (value < 0 || value > 5) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 to 5");
+        if (value < 0 || value > 7) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 to 7");
         c->opt_projector = value;
         return ACU_OK;
     case 8:

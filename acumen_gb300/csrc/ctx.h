@@ -49,7 +49,7 @@ struct DevBuf {
 template <typename Real>
 struct GeomSet {
     bool ready = false;
-    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_tw, fp_order, xsc_bp, xsc_fp;
+    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_tw, fp_order, lines_order, xsc_bp, xsc_fp;
     std::vector<float4> hx_bp;   // host copy of xsc_bp
     std::vector<float4> hs_bp;   // host copy of sc_bp as (sin, cos, 0, 0) (single precision)
     DevGeom<Real> d;
@@ -92,14 +92,16 @@ struct acu_ctx {
     int opt_refresh = 5;     // radon(uk): 1 recomputed every outer iteration (reference), K >= 2 every K-th, 0 never
     int opt_residual = 1;    // 1 initial CG residual from one backprojection of fk - radon(uk), 0 two (reference)
     int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions
-    int opt_projector = 5;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 row-parity
-                             // loads, 3 taps reused, 4 reuse + clipped steps, 5 the same with paired FMAs
+    int opt_projector = 7;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 row-parity
+                             // loads, 3 taps reused, 4 reuse + clipped steps, 5 the same with paired FMAs,
+                             // 6 pixel lines, 7 automatic (6 or 5 by how full the 32-slice lines are)
     std::string err;
     acu::GeomSet<float> g32;
     acu::GeomSet<double> g64;
     // operator work buffers
     acu::DevBuf w_in, w_out, w_q, w_host_in, w_host_out;
     acu::DevBuf pairP, pairPT;   // pair images of the single-precision projector
+    acu::DevBuf lineL, lineA;    // line image and ray sums of projector variant 6
     acu::DevBuf w_part;          // FP64 / int64 partial sums of the preprocessing reductions
     acu::TvState<float> tv32;
     acu::TvState<double> tv64;

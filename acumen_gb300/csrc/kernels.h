@@ -29,6 +29,8 @@ struct DevGeom {
     const double2* fft_tw64 = nullptr;
     int fft_L = 0, fft_log2L = 0;
     const int* fp_order = nullptr;  // [T] projector angles, |sin| >= |cos| first
+    const int* lines_order = nullptr;  // [T] projector angles, sin >= 0 first (lines_nup of them)
+    int lines_nup = 0;
     // exact positions (single precision only): split FP64 angle tables,
     // [T] x (s_a, c_a, s_r, c_r); exact != 0 selects them
     const float4* xsc_bp = nullptr;
@@ -56,6 +58,14 @@ void launch_radon_pairs(const DevGeom<float>& g, int G, const float* img, float*
 // steps limited to those that can meet a valid cell.
 void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float* IT, float* sino, cudaStream_t st,
                         bool par = false, bool reuse = false, bool clip = false, bool f2 = false);
+// Projector variant 6 (kernels_lines.cu): the batch regrouped into 128-byte
+// pixel lines of 32 slices, walked in bands of rows that stay in L2.  L and A
+// are work buffers of lines_image_floats and lines_sums_floats floats.
+void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float* L, float* A, float* sino,
+                        cudaStream_t st);
+size_t lines_image_floats(int N, int G);
+size_t lines_sums_floats(int N, int T, int G);
+int lines_band_rows(int N);
 // The staggered projector for one slice per thread (plain layout); IT is a
 // work buffer of N * N floats per slice.
 void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, float* IT, float* sino, cudaStream_t st);

@@ -8,9 +8,10 @@ Inputs are seeded synthetic sinograms (random-ellipse phantoms, analytic
 projections, Poisson counts at I0 = 5e3): the reference's neutron-CT datasets
 are not available.
 
-A "step" is one Bregman outer iteration of the whole batch (10 CG steps: 11
-projector and 11 filtered-backprojection launches plus the fused element-wise
-kernels, replayed as one CUDA graph).  value = S / (t_warm + nouter * t_step):
+A "step" is one Bregman outer iteration of the whole batch (10 CG steps: 10
+projections (11 every fifth iteration, which recomputes radon(uk)) and 11
+filtered backprojections plus the fused element-wise kernels, replayed as one
+CUDA graph).  value = S / (t_warm + nouter * t_step):
 slices per second of the full 50-iteration reconstruction with the inputs
 resident in HBM (t_warm = the FBP warm start, timed once).  e2e = the same
 through the host-buffer C ABI call acu_tvopt (pinned host input and outputs,
@@ -39,11 +40,32 @@ METRIC = "TV slices/sec 2048²@1200 angles batched vs plain GPU at relL2≤1e-4;
 N_GRID, T_ANG, S_BATCH = 2049, 1200, 256
 NINNER, NCG, NOUTER, LAM, MU, WPU = 1, 10, 50, 0.05, 1.0, 100
 POSITIONS = {"reference": 0, "exact": 1}   # ACU_OPT_POSITIONS values
-# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one projector
-# launch (k_radon_stag_reuse<4, exact, f32x2> plus its k_make_transpose) per group of
-# 4 slices at 2049^2 x 1200 angles, from one ncu capture of a 4-slice launch
-# (scaled by groups below)
-RADON_TRAFFIC_PER_GROUP = (298.25e6 + 37.49e6) + (67.22e6 + 17.71e6)
+# DRAM bytes (dram__bytes_read.sum + dram__bytes_write.sum) of one projection
+# by the pixel-line projector (k_lines_from_lanes, the 17 band launches of
+# k_radon_lines, k_lines_finish) per 32-slice line group at 2049^2 x 1200
+# angles, from one ncu capture of a 32-slice projection (scaled by line groups
+# below): 5.19 GB read + 3.25 GB written, mostly the ray sums' round trips
+# between the 17 band launches
+RADON_TRAFFIC_PER_LINE_GROUP = 5189434368 + 3248563968
+
+
+def projector_variant(option, S):
+    """The 4-slice projector variant the library runs for S slices
+    (ACU_OPT_PROJECTOR; 7 = automatic, as csrc/api.cu projector_variant)."""
+    G = (S + 3) // 4
+    if option != 7:
+        return option
+    return 6 if 8 * ((G + 7) // 8) <= G + G // 8 else 5
+
+
+def radon_launches(variant, N):
+    """Kernels of one batched projection: line conversion, one launch per
+    band of rows and the finish for the pixel-line projector (csrc/kernels_lines.cu
+    lines_band_rows); transpose and projector for the others."""
+    if variant != 6:
+        return 2
+    H = max(16, (32 << 20) // (N * 128) - 1)
+    return 2 + max(1, (N - 2 + H - 1) // H)
 
 
 def parse():
@@ -445,10 +467,10 @@ def main():
     t_step = e0.elapsed_time(e1) / 1000.0 / args.steps
     t_step, t_warm = max_over_ranks([t_step, t_warm], world, "cuda")
     value = job_value(world, S, t_warm, t_step)
-    # kernels of one outer iteration (the captured graph): transpose + projector
-    # per radon, filter + backprojection per iradon, and the element-wise /
-    # finaliser kernels (100 for ninner=1, ncg=10 with the merged initial
-    # residual, 101 with the reference's two backprojections)
+    # kernels of one outer iteration (the captured graph): the projector's
+    # launches per radon, filter + backprojection per iradon, and the
+    # element-wise / finaliser kernels (100 for ninner=1, ncg=10 with the
+    # merged initial residual, 101 with the reference's two backprojections)
     merged = t.get_option(9) == 1
     refresh = t.get_option(11)        # radon(uk) recomputed every refresh-th outer iteration
     carried = refresh != 1
@@ -458,7 +480,9 @@ def main():
     n_iradon = NINNER * ((1 if merged else 2) + NCG)
     n_ew = NINNER * ((5 if merged else 4) + 5 * NCG) + 1
     n_ew += NINNER * NCG if carried else 0          # the sinogram updates ruk += alpha radon(p)
-    kernel_launches = (2 * n_radon + 2 * n_iradon + n_ew) * args.steps + 2 * n_full
+    variant = projector_variant(t.get_option(7), S)
+    per_radon = radon_launches(variant, N)
+    kernel_launches = (per_radon * n_radon + 2 * n_iradon + n_ew) * args.steps + per_radon * n_full
 
     line = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True, "scaling": "weak",
@@ -480,14 +504,18 @@ def main():
         hbm, kind = measured_peaks()
         alg_bytes = 4.0 * (N * N + N * T) * S
         achieved = alg_bytes / t_radon / 1e9
-        groups = (S + 3) // 4
-        traffic = RADON_TRAFFIC_PER_GROUP * groups if (N, T) == (N_GRID, T_ANG) else None
-        line["roofline"] = {"bound": "hbm", "kernel": "k_radon_stag_reuse<4, exact, f32x2> (projector, tv_hpc.F90:137-156)",
+        line_groups = ((S + 3) // 4 + 7) // 8
+        traffic = (RADON_TRAFFIC_PER_LINE_GROUP * line_groups
+                   if (N, T) == (N_GRID, T_ANG) and variant == 6 and RADON_TRAFFIC_PER_LINE_GROUP else None)
+        kname = ("k_radon_lines (pixel lines of 32 slices, %d band launches + conversions; projector, "
+                 "tv_hpc.F90:137-156)" % (radon_launches(6, N) - 2) if variant == 6 else
+                 "k_radon_stag_reuse<4, exact, f32x2> (projector, tv_hpc.F90:137-156)")
+        line["roofline"] = {"bound": "hbm", "kernel": kname,
                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                             "peak_kind": kind, "traffic": traffic,
                             "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,
-                            "note": "bound by L1 data-pipe wavefronts (ncu 91 %), not by HBM (runs from L2); "
-                                    "traffic from one 4-slice ncu capture scaled by slice groups",
+                            "note": "runs from L2 and L1, not from HBM (each band of rows stays in L2); "
+                                    "traffic from one 32-slice ncu capture scaled by 32-slice line groups",
                             "l1_level": l1_level(16.0 * N * N * T * S / t_radon / 1e9, clocks,
                                                  bytes_per_sample_slice=16,
                                                  sample_slices_per_s=N * N * T * S / t_radon)}

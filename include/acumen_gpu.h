@@ -68,7 +68,9 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
                                  2 the same with the taps loaded by row parity, 3 the same with the taps
                                  of the previous sample reused, 4 reuse with each warp's steps limited
                                  to those that can meet a valid cell, 5 the same with paired FP32 FMAs
-                                 (fma.rn.f32x2; default); 1 and 3 to 5 give identical results */
+                                 (fma.rn.f32x2), 6 pixel lines of 32 slices walked in bands of rows,
+                                 7 automatic (default): 6 when the batch fills its 32-slice lines to
+                                 8/9 or more, else 5; 1 and 3 to 6 give identical results */
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 0 the reference's arithmetic (default), 1 exact */
 #define ACU_OPT_RESIDUAL 9    /* batched TV: the initial CG residual mu*iradon(fk) - mu*iradon(radon(uk)) as
                                  1 one backprojection of fk - radon(uk) (default), or 0 the reference's two */

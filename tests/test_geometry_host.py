@@ -105,3 +105,51 @@ def test_step_clipping_keeps_every_valid_sample(N):
             idx = np.nonzero(ok)[0] + 1
             if idx.size:
                 assert lo <= idx.min() and idx.max() <= hi, (th, jy, lo, hi, idx.min(), idx.max())
+
+
+def band_steps(s, c, dy, mid, N, ylo, yhi, lo, hi):
+    """float32 restatement of band_steps (csrc/kernels_lines.cu)."""
+    off = f32(mid + f32(c * dy))
+    y0, y1 = f32(ylo - 1), f32(yhi + 2)
+    if abs(s) < f32(1e-3):
+        climb = f32(abs(s) * f32(N)) + f32(2)
+        if off + climb < y0 or off - climb > y1:
+            return 1, 0
+        return lo, hi
+    t0, t1 = (y0 - off) / s, (y1 - off) / s
+    return max(lo, int(np.floor(f32(min(t0, t1) + mid))) - 2), min(hi, int(np.ceil(f32(max(t0, t1) + mid))) + 2)
+
+
+@pytest.mark.parametrize("N, H", [(64, 7), (129, 16), (300, 41)])
+def test_band_walk_visits_every_sample_once_in_step_order(N, H):
+    """Projector variant 6 walks the cell rows 2..N-1 in bands of H rows: each
+    valid sample of a ray lies in the step range that band_steps keeps for
+    exactly the band of its cell row, and the bands in launch order (upward
+    for sin >= 0, downward otherwise) meet a ray's samples in step order."""
+    mid = f32((N + 1) // 2)
+    nb = max(1, (N - 2 + H - 1) // H)
+    ths = np.concatenate([syn.angles(29), [90.0, 0.0, 45.0, 135.0, 89.9999, 90.0001, 1e-5, 179.99]]).astype(np.float32)
+    pi = f32(4) * np.arctan(f32(1))
+    jx = np.arange(1, N + 1, dtype=np.float32)
+    dxv = jx - mid
+    for th in ths:
+        ct = (pi * (th - f32(90))) / f32(180)
+        s, c = f32(np.sin(ct)), f32(np.cos(ct))
+        for jy in range(1, N + 1, max(1, N // 40)):
+            dy = f32(jy) - mid
+            lo, hi = valid_steps(s, c, dy, mid, N)
+            xr = (c * dxv - s * dy) + mid
+            yr = (s * dxv + c * dy) + mid
+            x1, y1 = np.floor(xr).astype(int), np.floor(yr).astype(int)
+            ok = (np.minimum(x1, y1) > 1) & (np.maximum(x1, y1) < N)
+            seen = []
+            for k in range(nb):
+                b = k if s >= 0 else nb - 1 - k
+                ylo, yhi = 2 + b * H, min(N - 1, 1 + (b + 1) * H)
+                blo, bhi = band_steps(s, c, dy, mid, N, ylo, yhi, lo, hi)
+                inband = ok & (y1 >= ylo) & (y1 <= yhi)
+                idx = np.nonzero(inband)[0] + 1
+                if idx.size:
+                    assert blo <= idx.min() and idx.max() <= bhi, (th, jy, b, blo, bhi, idx.min(), idx.max())
+                seen.extend(idx.tolist())
+            assert seen == (np.nonzero(ok)[0] + 1).tolist(), (th, jy)

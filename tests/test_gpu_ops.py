@@ -167,12 +167,13 @@ def test_projector_variants_agree(case, oracle):
     for x in (case["img"][:5].astype(np.float32), rng.standard_normal((5, case["N"], case["N"])).astype(np.float32)):
         img = torch.from_numpy(x).cuda()
         outs = []
-        for v in (0, 1, 2, 3, 4, 5):
+        for v in range(7):
             t.set_option(7, v)
             outs.append(t.radon(img))
         # reusing the previous sample's taps, skipping steps that cannot meet
-        # a valid cell and pairing the FMAs change neither values nor order
-        assert all(torch.equal(outs[v], outs[1]) for v in (3, 4, 5))
+        # a valid cell, pairing the FMAs and walking the rays in bands of
+        # pixel lines change neither values nor order
+        assert all(torch.equal(outs[v], outs[1]) for v in range(3, 7))
         ref = oracle.radon(x, case["th"], 32)
         for o in outs:
             assert rel(o, ref) < 1e-6
@@ -215,7 +216,7 @@ def test_exact_positions_projector_and_adjoint(oracle, built_lib):
     xc = torch.from_numpy(x).cuda()
     e_ref = rel(t.radon(xc), ref64)
     t.set_option(8, 1)
-    for proj in (5, 4, 3, 2, 1, 0):
+    for proj in (6, 5, 4, 3, 2, 1, 0):
         t.set_option(7, proj)
         e4 = rel(t.radon(xc), ref64)                      # batched, 4 slices per thread
         assert e4 < 3e-6 and e4 < e_ref / 5, (proj, e4, e_ref)
@@ -227,6 +228,27 @@ def test_exact_positions_projector_and_adjoint(oracle, built_lib):
     lhs = torch.sum(t.radon(xp).double() * y.double()).item()
     rhs = torch.sum(xp.double() * t.radon_adjoint(y).double()).item()
     assert abs(lhs - rhs) <= 1e-6 * abs(lhs)
+
+
+@pytest.mark.parametrize("N, T, S, wpu", [(725, 97, 37, 20), (1025, 60, 4, 30), (2049, 24, 33, 100), (64, 37, 9, 6),
+                                           (3, 11, 4, 1)])
+def test_line_projector_bitwise(N, T, S, wpu):
+    """Projector variant 6 (pixel lines of 32 slices, rays walked in bands of
+    rows, several bands from N = 725 on) gives bit for bit the sums of the
+    default variant 5, in both position modes, on random images that reach the
+    border, with slice counts that leave super-groups partly empty and
+    angles on and near the axes."""
+    th = np.concatenate([syn.angles(T - 8), [0.0, 45.0, 90.0, 135.0, 180.0, 89.9999, 90.0001, 1e-5]])
+    th = th.astype(np.float32)
+    t = Tomography(N, th, wpu)
+    x = torch.from_numpy(np.random.default_rng(N + S).standard_normal((S, N, N)).astype(np.float32)).cuda()
+    for ex in (0, 1):
+        t.set_option(8, ex)
+        t.set_option(7, 5)
+        ref = t.radon(x)
+        t.set_option(7, 6)
+        got = t.radon(x)
+        assert torch.equal(got, ref), (ex, (got - ref).abs().max().item())
 
 
 def test_backprojection_groups_per_thread(oracle, built_lib):

@@ -141,6 +141,20 @@ def test_graph_follows_projector_option(prob):
     assert torch.equal(tv0, ref0)
 
 
+def test_line_projector_in_the_solver(prob):
+    """The captured outer iteration with projector variant 6 gives bit for
+    bit the TV result of the default variant 5 (the projector sums agree
+    bit for bit), with a batch that fills one 32-slice super-group partly."""
+    a = prob["args"]
+    f = torch.from_numpy(prob["f"][:6]).cuda()
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    t.set_option(7, 5)
+    ref, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    t.set_option(7, 6)
+    got, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    assert torch.equal(got, ref)
+
+
 def test_merged_residual_matches_reference_order(prob):
     """ACU_OPT_RESIDUAL: the initial CG residual from one backprojection of
     fk - radon(uk) (default) against the reference's mu*iradon(fk) -
