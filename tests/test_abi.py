@@ -50,3 +50,23 @@ def test_python_mirror_raises_on_missing_library(tmp_path, monkeypatch):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(RuntimeError, match="no CPU fallback"):
         _lib.lib()
+
+
+def header_constants():
+    txt = "".join(open(h).read() for h in glob.glob(os.path.join(ROOT, "include", "*.h")))
+    return {k: int(v) for k, v in re.findall(r"^#define\s+(ACU_(?:OPT|ERR)_\w+|ACU_OK)\s+\(?(-?\d+)\)?", txt, re.M)}
+
+
+def test_binding_constants_match_the_header():
+    """The option and status numbers of the Python mirror (_lib.py) and of the
+    Fortran module (fortran/acumen_gpu.f90) are the header's, and each binding
+    names every option the header defines."""
+    from acumen_gb300 import _lib
+    consts = header_constants()
+    assert consts["ACU_OPT_PROJECTOR"] == 7 and consts["ACU_ERR_INVALID"] == -1
+    for k, v in consts.items():
+        assert getattr(_lib, k) == v, k
+    f90 = open(os.path.join(ROOT, "acumen_gb300", "fortran", "acumen_gpu.f90")).read()
+    fparams = {k: int(v) for k, v in re.findall(r"(ACU_\w+)\s*=\s*(-?\d+)", f90)}
+    for k, v in consts.items():
+        assert fparams.get(k) == v, k
