@@ -514,8 +514,9 @@ def main():
                             "achieved": achieved, "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                             "peak_kind": kind, "traffic": traffic,
                             "algorithmic_bytes": alg_bytes, "launch_ms": 1000 * t_radon,
-                            "note": "runs from L2 and L1, not from HBM (each band of rows stays in L2); "
-                                    "traffic from one 32-slice ncu capture scaled by 32-slice line groups",
+                            "note": "runs from L2 and L1, not from HBM (each band of rows stays in L2); traffic (from "
+                                    "one 32-slice ncu capture, scaled by 32-slice line groups) is mostly the ray "
+                                    "sums carried between the band launches, ~1.4 % of the HBM bandwidth",
                             "l1_level": l1_level(16.0 * N * N * T * S / t_radon / 1e9, clocks,
                                                  bytes_per_sample_slice=16,
                                                  sample_slices_per_s=N * N * T * S / t_radon)}
