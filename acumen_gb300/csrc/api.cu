@@ -566,7 +566,9 @@ int tv_chunk(acu_ctx* c, int S, bool host_io)
     // projector's work buffers (transposed copy; pair images for variant 0;
     // line image and ray sums for variant 6), and the host-buffer entry
     // point's device copies of f, tv and fbp
-    const int proj = projector_variant(c, (S + 3) / 4);
+    // the automatic projector choice can differ between the call and a
+    // chunk of it: count the larger (pixel-line) buffers then
+    const int proj = c->opt_projector == 7 ? 6 : c->opt_projector;
     size_t per = sizeof(Real) * (5 * T * N + 10 * N * N);
     if (sizeof(Real) == 4) per += sizeof(float) * (proj == 0 ? 4 * N * N : proj == 6 ? N * N + T * N : N * N);
     if (host_io) per += sizeof(float) * (T * N + 2 * N * N);
