@@ -32,7 +32,7 @@ struct BatchDev {
     const float* sc_fp = nullptr;
     const float4* xsc_bp = nullptr;   // exact-position tables, [angle][4] (index ProbDesc::sc / 2)
     const float4* xsc_fp = nullptr;
-    int exact = 0;                    // 1: exact sample positions (acu_batch_set_option)
+    int exact = 1;                    // 1: exact sample positions (default), 0: the reference's (acu_batch_set_option)
     const float* cmask = nullptr;
     const float* fft_h = nullptr;
     const float2* tw = nullptr;   // twiddles of the largest L (Lmax entries)

@@ -91,7 +91,7 @@ struct acu_ctx {
     int opt_max_batch = 0;   // slices per device batch of the TV solver: 0 as many as fit
     int opt_refresh = 5;     // radon(uk): 1 recomputed every outer iteration (reference), K >= 2 every K-th, 0 never
     int opt_residual = 1;    // 1 initial CG residual from one backprojection of fk - radon(uk), 0 two (reference)
-    int opt_positions = 0;   // 0 the reference's single-precision positions, 1 exact positions
+    int opt_positions = 1;   // 1 exact positions (default), 0 the reference's single-precision positions
     int opt_projector = 7;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 row-parity
                              // loads, 3 taps reused, 4 reuse + clipped steps, 5 the same with paired FMAs,
                              // 6 pixel lines, 7 automatic (6 or 5 by how full the 32-slice lines are)

@@ -8,6 +8,10 @@
 // Arithmetic that decides an index or a comparison is written with explicit
 // round-to-nearest operations so that it matches the single-precision
 // reference operation for operation.
+#include <climits>
+#include <cmath>
+
+#include "../../include/acumen_gpu.h"
 #include "common.cuh"
 #include "prep.h"
 
@@ -155,46 +159,90 @@ __global__ void k_sum_partials(const double* __restrict__ part, int n, int strid
 
 // ---- cross-correlation registration (new) --------------------------------------
 // C(k) = sum_{x,y} p0(x,y) * p180(ndet-1-x+k, y) with every product truncated
-// to 2^-32 fixed point: integer sums do not depend on their order, so the
-// argmax is bit-exact against the CPU oracle.
-__device__ __forceinline__ long long fx_prod(float a, float b)
+// to 2^-32 fixed point and summed exactly in 128-bit integers: integer sums do
+// not depend on their order, so the argmax is bit-exact against the CPU oracle,
+// and a 128-bit sum of n terms below 2^63 cannot wrap for n < 2^64.  A product
+// that is not finite or not below 2^31 in magnitude (its fixed-point value would
+// not fit 64 bits) sets the range flag and is left out; the host then rejects
+// the input.  Every element of p0 and p180 meets a partner at k = 0, so every
+// element is checked.
+//
+// Scratch layout (unsigned 64-bit words): lag i's sum at [2i] (low word) and
+// [2i+1] (high word, two's complement), then one word holding the argmax
+// index (low 32 bits) and the range flag (high 32 bits).
+constexpr double kFixScale = 4294967296.0;     // 2^32
+constexpr double kFixLimit = 2147483648.0;     // |product| < 2^31
+
+// 128-bit atomic add from two 64-bit atomics: the low words add modulo 2^64
+// and each addition that wraps carries one into the high word, so the pair
+// holds the exact sum modulo 2^128 whatever the order of the additions.
+__device__ __forceinline__ void atomic_add_i128(unsigned long long* w, __int128 v)
 {
-    const double p = (double)a * (double)b;
-    return __double2ll_rd(p * 4294967296.0);
+    const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
+    const unsigned long long old = atomicAdd(w, lo);
+    const unsigned long long carry = (old + lo < old) ? 1ull : 0ull;
+    if (hi + carry) atomicAdd(w + 1, hi + carry);
+}
+
+__device__ __forceinline__ __int128 shfl_down_i128(__int128 v, int o)
+{
+    const unsigned long long lo = __shfl_down_sync(0xffffffffu, (unsigned long long)v, o);
+    const long long hi = __shfl_down_sync(0xffffffffu, (long long)(v >> 64), o);
+    return ((__int128)hi << 64) | (__int128)lo;
 }
 
 __global__ void __launch_bounds__(256) k_xcorr(int ndet, int nrows, int kmax, const float* __restrict__ p0,
-                                               const float* __restrict__ p180, unsigned long long* __restrict__ corr)
+                                               const float* __restrict__ p180, unsigned long long* __restrict__ w)
 {
     const int k = (int)blockIdx.y - kmax;
     const long n = (long)ndet * nrows;
-    long long acc = 0;
+    __int128 acc = 0;
+    bool bad = false;
     for (long i = blockIdx.x * (long)blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x) {
         const int x = (int)(i % ndet), y = (int)(i / ndet);
         const int xm = ndet - 1 - x + k;
-        if (xm >= 0 && xm < ndet) acc += fx_prod(p0[i], p180[(size_t)y * ndet + xm]);
+        if (xm >= 0 && xm < ndet) {
+            const double p = (double)p0[i] * (double)p180[(size_t)y * ndet + xm];   // exact
+            if (fabs(p) < kFixLimit) acc += (__int128)__double2ll_rd(p * kFixScale);
+            else bad = true;                                                          // also NaN
+        }
     }
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
-    if ((threadIdx.x & 31) == 0) atomicAdd(&corr[blockIdx.y], (unsigned long long)acc);
+    for (int o = 16; o > 0; o >>= 1) acc += shfl_down_i128(acc, o);
+    if ((threadIdx.x & 31) == 0 && acc != 0) atomic_add_i128(&w[2 * blockIdx.y], acc);
+    if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) {
+        unsigned int* flag = reinterpret_cast<unsigned int*>(w + 2 * (2 * kmax + 1)) + 1;
+        atomicOr(flag, 1u);
+    }
 }
 
-// Warp-shuffle argmax over the nk correlation values (ties: lowest index).
-__global__ void k_argmax(int nk, const unsigned long long* __restrict__ corr, int* __restrict__ best)
+__device__ __forceinline__ bool i128_better(long long ah, unsigned long long al, int ai, long long bh,
+                                            unsigned long long bl, int bi)
 {
-    long long bv = LLONG_MIN;
+    if (ah != bh) return ah > bh;
+    if (al != bl) return al > bl;
+    return ai < bi;
+}
+
+// Warp-shuffle argmax over the nk 128-bit correlation values (ties: lowest index).
+__global__ void k_argmax(int nk, unsigned long long* __restrict__ w)
+{
+    long long bh = LLONG_MIN;
+    unsigned long long bl = 0;
     int bi = 0x7fffffff;
     for (int i = threadIdx.x; i < nk; i += 32) {
-        const long long v = (long long)corr[i];
-        if (v > bv || (v == bv && i < bi)) { bv = v; bi = i; }
+        const long long h = (long long)w[2 * i + 1];
+        const unsigned long long l = w[2 * i];
+        if (i128_better(h, l, i, bh, bl, bi)) { bh = h; bl = l; bi = i; }
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
-        const long long ov = __shfl_down_sync(0xffffffffu, bv, o);
+        const long long oh = __shfl_down_sync(0xffffffffu, bh, o);
+        const unsigned long long ol = __shfl_down_sync(0xffffffffu, bl, o);
         const int oi = __shfl_down_sync(0xffffffffu, bi, o);
-        if (ov > bv || (ov == bv && oi < bi)) { bv = ov; bi = oi; }
+        if (i128_better(oh, ol, oi, bh, bl, bi)) { bh = oh; bl = ol; bi = oi; }
     }
-    if (threadIdx.x == 0) best[0] = bi;
+    if (threadIdx.x == 0) reinterpret_cast<int*>(w + 2 * nk)[0] = bi;
 }
 
 // ---- 27-point median (:426-452): the reference's descending exchange sort,
@@ -314,14 +362,76 @@ void launch_com(int ndet, int nrows, const float* p0, const float* p180, double*
     k_com<<<nblk, 256, 0, st>>>(ndet, nrows, ndet % 2 == 0 ? 1 : 0, p0, p180, part);
     for (int j = 0; j < 3; ++j) k_sum_partials<<<1, 256, 0, st>>>(part, nblk, 3, j, out3 + j);
 }
-void launch_xcorr(int ndet, int nrows, int kmax, const float* p0, const float* p180, unsigned long long* corr,
-                  int* best, cudaStream_t st)
+size_t xcorr_scratch_words(int kmax) { return 2 * (size_t)(2 * kmax + 1) + 1; }
+
+namespace {
+template <typename T>
+struct same_t {
+    using type = T;
+};
+// cudaLaunchKernel with typed arguments: returns this launch's own error and
+// leaves earlier, unrelated errors of the caller pending.
+template <typename... P>
+cudaError_t launch_k(void (*k)(P...), dim3 grd, dim3 blk, cudaStream_t st, typename same_t<P>::type... args)
+{
+    void* a[] = {&args...};
+    return cudaLaunchKernel(reinterpret_cast<const void*>(k), grd, blk, a, 0, st);
+}
+}  // namespace
+
+cudaError_t launch_xcorr(int ndet, int nrows, int kmax, const float* p0, const float* p180,
+                         unsigned long long* scratch, cudaStream_t st)
 {
     const int nk = 2 * kmax + 1;
-    cudaMemsetAsync(corr, 0, sizeof(unsigned long long) * nk, st);
+    cudaError_t e = cudaMemsetAsync(scratch, 0, sizeof(unsigned long long) * xcorr_scratch_words(kmax), st);
+    if (e != cudaSuccess) return e;
     dim3 grd(nblocks((long)ndet * nrows, 256, 64), nk);
-    k_xcorr<<<grd, 256, 0, st>>>(ndet, nrows, kmax, p0, p180, corr);
-    k_argmax<<<1, 32, 0, st>>>(nk, corr, best);
+    e = launch_k(k_xcorr, grd, dim3(256), st, ndet, nrows, kmax, p0, p180, scratch);
+    if (e != cudaSuccess) return e;
+    return launch_k(k_argmax, dim3(1), dim3(32), st, nk, scratch);
+}
+
+int xcorr_finish(int kmax, const unsigned long long* h, int64_t* corr_out, int* k_best, double* k_sub,
+                 const char** why)
+{
+    const int nk = 2 * kmax + 1;
+    const int bi = (int)(unsigned int)(h[2 * nk] & 0xffffffffu);
+    const unsigned int flag = (unsigned int)(h[2 * nk] >> 32);
+    if (flag) {
+        *why = "a projection holds a value that is not finite, or a product p0*p180 of magnitude >= 2^31";
+        return ACU_ERR_INVALID;
+    }
+    if (bi < 0 || bi >= nk) {
+        *why = "the correlation argmax is out of range";
+        return ACU_ERR_CUDA;
+    }
+    auto fits = [&](int i) {
+        const long long hi = (long long)h[2 * i + 1];
+        const long long lo = (long long)h[2 * i];
+        return hi == (lo < 0 ? -1ll : 0ll);
+    };
+    auto to_double = [&](int i) {   // the sum as a double (exact conversion of an int64 when it fits)
+        if (fits(i)) return (double)(long long)h[2 * i];
+        return ldexp((double)(long long)h[2 * i + 1], 64) + (double)h[2 * i];
+    };
+    if (corr_out) {
+        for (int i = 0; i < nk; ++i)
+            if (!fits(i)) {
+                *why = "a correlation sum exceeds the int64 range of corr_out (pass corr_out = NULL for the lag "
+                       "alone)";
+                return ACU_ERR_UNSUPPORTED;
+            }
+        for (int i = 0; i < nk; ++i) corr_out[i] = (int64_t)(long long)h[2 * i];
+    }
+    double frac = 0.0;
+    if (bi > 0 && bi < nk - 1) {
+        const double cm = to_double(bi - 1), c0 = to_double(bi), cp = to_double(bi + 1);
+        const double den = cm - 2.0 * c0 + cp;
+        if (den < 0.0) frac = 0.5 * (cm - cp) / den;
+    }
+    *k_best = bi - kmax;
+    *k_sub = (double)(bi - kmax) + frac;
+    return ACU_OK;
 }
 void launch_median27(int ndet, int nrows, int nchunk, int p_first, int nfiles, const float* proj, float* out,
                      cudaStream_t st)

@@ -22,8 +22,16 @@ void launch_mirror_error(int ndet, int nrows, const float* p0, const float* p180
 // writes tm, cmx_0, cmx_180 to out3[0..2]; part holds 3 * nblk partials
 void launch_com(int ndet, int nrows, const float* p0, const float* p180, double* part, int nblk, double* out3,
                 cudaStream_t st);
-void launch_xcorr(int ndet, int nrows, int kmax, const float* p0, const float* p180, unsigned long long* corr,
-                  int* best, cudaStream_t st);
+// Cross-correlation registration: scratch holds xcorr_scratch_words(kmax)
+// 64-bit words (per-lag 128-bit sums, argmax index and range flag); the
+// launcher clears it first and returns the first failing call's error.
+// xcorr_finish turns a host copy of the scratch into the results (ACU_OK, or
+// an ACU_ERR_* code with the reason in *why).
+size_t xcorr_scratch_words(int kmax);
+cudaError_t launch_xcorr(int ndet, int nrows, int kmax, const float* p0, const float* p180,
+                         unsigned long long* scratch, cudaStream_t st);
+int xcorr_finish(int kmax, const unsigned long long* scratch, int64_t* corr_out, int* k_best, double* k_sub,
+                 const char** why);
 void launch_median27(int ndet, int nrows, int nchunk, int p_first, int nfiles, const float* proj, float* out,
                      cudaStream_t st);
 void launch_resample_to_sino(int ndet, int nrows, int nchunk, int p_first, int nfiles, const float* med,

@@ -212,27 +212,16 @@ int acu_xcorr_register_dev(acu_ctx* c, int ndet, int nrows, const float* d_p0, c
     CKRET(check_proj(c, ndet, nrows));
     if (!d_p0 || !d_p180 || !k_best || !k_sub || kmax < 1 || kmax > 4096)
         return set_err(c, ACU_ERR_INVALID, "invalid cross-correlation arguments (kmax %d)", kmax);
-    const int nk = 2 * kmax + 1;
-    CK(c, c->w_part.ensure(sizeof(unsigned long long) * (nk + 4)));
-    unsigned long long* corr = c->w_part.as<unsigned long long>();
-    int* best = reinterpret_cast<int*>(corr + nk);
-    launch_xcorr(ndet, nrows, kmax, d_p0, d_p180, corr, best, c->stream);
-    CKLAUNCH(c);
-    std::vector<long long> h(nk);
-    int bi = 0;
-    CK(c, cudaMemcpyAsync(h.data(), corr, sizeof(long long) * nk, cudaMemcpyDeviceToHost, c->stream));
-    CK(c, cudaMemcpyAsync(&bi, best, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    const size_t nw = xcorr_scratch_words(kmax);
+    CK(c, c->w_part.ensure(sizeof(unsigned long long) * nw));
+    unsigned long long* w = c->w_part.as<unsigned long long>();
+    CK(c, launch_xcorr(ndet, nrows, kmax, d_p0, d_p180, w, c->stream));
+    std::vector<unsigned long long> h(nw);
+    CK(c, cudaMemcpyAsync(h.data(), w, sizeof(unsigned long long) * nw, cudaMemcpyDeviceToHost, c->stream));
     CK(c, cudaStreamSynchronize(c->stream));
-    double frac = 0.0;
-    if (bi > 0 && bi < nk - 1) {
-        const double cm = (double)h[bi - 1], c0 = (double)h[bi], cp = (double)h[bi + 1];
-        const double den = cm - 2.0 * c0 + cp;
-        if (den < 0.0) frac = 0.5 * (cm - cp) / den;
-    }
-    *k_best = bi - kmax;
-    *k_sub = (double)(bi - kmax) + frac;
-    if (corr_out)
-        for (int i = 0; i < nk; ++i) corr_out[i] = h[i];
+    const char* why = "";
+    const int rc = xcorr_finish(kmax, h.data(), corr_out, k_best, k_sub, &why);
+    if (rc != ACU_OK) return set_err(c, rc, "cross-correlation registration: %s", why);
     return ACU_OK;
 }
 

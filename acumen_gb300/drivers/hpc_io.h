@@ -187,14 +187,16 @@ inline void check(int rc, acu_ctx* ctx)
     if (rc != ACU_OK) throw Fail(std::string("acumen_gpu: ") + acu_last_error(ctx));
 }
 
-// ACUMEN_POSITIONS=exact (or 1): single-precision sample positions from the
-// split FP64 angle tables (ACU_OPT_POSITIONS); default: the reference's.
+// ACUMEN_POSITIONS: single-precision sample positions (ACU_OPT_POSITIONS).
+// exact (or 1, the default): from the split FP64 angle tables, the mode that
+// meets relL2 <= 1e-5 (FBP) and 1e-4 (TV) against FP64 at the benchmark
+// sizes; reference (or 0): the reference's own single-precision arithmetic.
 inline void apply_positions(acu_ctx* ctx)
 {
     const std::string v = env("ACUMEN_POSITIONS", false);
-    if (v == "exact" || v == "1") check(acu_set_option(ctx, ACU_OPT_POSITIONS, 1), ctx);
-    else if (!v.empty() && v != "reference" && v != "0")
-        throw Fail("ACUMEN_POSITIONS must be 'reference' (0) or 'exact' (1), got '" + v + "'");
+    if (v.empty() || v == "exact" || v == "1") check(acu_set_option(ctx, ACU_OPT_POSITIONS, 1), ctx);
+    else if (v == "reference" || v == "0") check(acu_set_option(ctx, ACU_OPT_POSITIONS, 0), ctx);
+    else throw Fail("ACUMEN_POSITIONS must be 'reference' (0) or 'exact' (1), got '" + v + "'");
 }
 
 // Batches through read -> compute -> write with the file I/O of the next and

@@ -134,7 +134,9 @@ module Tomography_gpu
   real, public, dimension(:), allocatable :: theta
   real, public, dimension(:,:), allocatable :: f
   type(c_ptr), private :: ctx = c_null_ptr
-  integer, private :: ctx_ntheta = -1
+  ! the geometry the library context was created with
+  integer, private :: ctx_nimage = -1, ctx_ntheta = -1, ctx_wpu = -1
+  real, private, dimension(:), allocatable :: ctx_theta
 
 contains
 
@@ -149,16 +151,35 @@ contains
     if (.not. allocated(f)) allocate(f(nimage, ntheta))
   end subroutine int_radon
 
+  ! (Re)creates the library context when the grid, the angles or the mask
+  ! taper differ from the ones it was created with: a driver may change
+  ! theta, nimage or wpu between slices at the same ntheta.
   subroutine ensure_ctx()
-    if (c_associated(ctx) .and. ctx_ntheta == ntheta) return
-    if (c_associated(ctx)) call acu_check(acu_ctx_destroy(ctx), c_null_ptr)
+    logical :: same
+    same = .false.
+    if (c_associated(ctx)) then
+      if (ctx_nimage == nimage .and. ctx_ntheta == ntheta .and. ctx_wpu == wpu) then
+        same = all(ctx_theta == theta(1:ntheta))
+      end if
+      if (same) return
+      call acu_check(acu_ctx_destroy(ctx), c_null_ptr)
+      ctx = c_null_ptr
+    end if
     call acu_check(acu_ctx_create(ctx, int(nimage, c_int), int(ntheta, c_int), theta, int(wpu, c_int)), c_null_ptr)
+    ctx_nimage = nimage
     ctx_ntheta = ntheta
+    ctx_wpu = wpu
+    if (allocated(ctx_theta)) deallocate(ctx_theta)
+    allocate(ctx_theta(ntheta))
+    ctx_theta = theta(1:ntheta)
   end subroutine ensure_ctx
 
   subroutine fin_radon()
     if (c_associated(ctx)) call acu_check(acu_ctx_destroy(ctx), c_null_ptr)
     ctx = c_null_ptr
+    ctx_nimage = -1
+    ctx_ntheta = -1
+    ctx_wpu = -1
   end subroutine fin_radon
 
   ! tv_hpc.F90:84-126

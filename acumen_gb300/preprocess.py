@@ -87,13 +87,16 @@ class Preprocessor:
              ctypes.byref(th), ctypes.byref(sh), ctypes.byref(ne), ctx=self._h)
         return th.value, sh.value, ne.value
 
-    def xcorr_register(self, p0, p180, kmax):
+    def xcorr_register(self, p0, p180, kmax, want_corr=True):
+        """(k_best, k_sub, corr); corr is None with want_corr=False, which also
+        serves sums beyond the int64 range of corr_out."""
         nrows, ndet = p0.shape
-        corr = np.zeros(2 * kmax + 1, np.int64)
+        corr = np.zeros(2 * kmax + 1, np.int64) if want_corr else None
         kb, ks = ctypes.c_int(), ctypes.c_double()
         self._stream()
         call("acu_xcorr_register_dev", self._h, ndet, nrows, _ptr(p0.contiguous()), _ptr(p180.contiguous()),
-             int(kmax), corr.ctypes.data_as(ctypes.c_void_p), ctypes.byref(kb), ctypes.byref(ks), ctx=self._h)
+             int(kmax), corr.ctypes.data_as(ctypes.c_void_p) if want_corr else None, ctypes.byref(kb),
+             ctypes.byref(ks), ctx=self._h)
         return kb.value, ks.value, corr
 
     # :426-452

@@ -326,44 +326,68 @@ void orc_proj_to_sino(int nfiles, int ndet, int nrows, const float *proj, float 
 /* sub-pixel axis offset).  Not in the reference.                           */
 /* ====================================================================== */
 
-/* Products are accumulated as 2^-32 fixed point in int64 so that the sums,
- * and hence the integer argmax, do not depend on summation order.          */
-static inline int64_t fx_prod(float a, float b)
+/* Products are truncated to 2^-32 fixed point and summed exactly in 128-bit
+ * integers, so that the sums, and hence the integer argmax, do not depend on
+ * summation order and cannot wrap.  A product that is not finite or not below
+ * 2^31 in magnitude is out of range: the call returns 1 and leaves the
+ * outputs unset (the library returns ACU_ERR_INVALID for the same inputs). */
+typedef __int128 orc_i128;
+
+/* The sum as a double: an exact int64 conversion when it fits int64, else
+ * hi * 2^64 + lo (the library's conversion). */
+static double i128_to_double(orc_i128 v)
 {
-    double p = (double)a * (double)b;          /* exact: 24x24-bit product */
-    return (int64_t)floor(p * 4294967296.0);
+    if (v >= (orc_i128)INT64_MIN && v <= (orc_i128)INT64_MAX) return (double)(int64_t)v;
+    return ldexp((double)(int64_t)(v >> 64), 64) + (double)(uint64_t)v;
 }
 
 /* C(k) = sum_{x,y} p0(x,y) * p180(ndet-1-x+k, y), k = -kmax..kmax (0-based x);
  * terms with the mirrored index outside [0,ndet) are skipped.  Returns the
  * integer argmax (lowest k on ties) and the parabolic sub-pixel vertex.
- * The axis offset from the detector centre is (k + frac)/2 pixels.         */
-void orc_xcorr_register(int ndet, int nrows, const float *p0, const float *p180, int kmax,
-                        int64_t *corr, int *k_best, double *k_sub)
+ * The axis offset from the detector centre is (k + frac)/2 pixels.  corr
+ * receives the sums as int64; returns 2 if one does not fit (the library's
+ * ACU_ERR_UNSUPPORTED when corr_out is requested), 1 on out-of-range input. */
+int orc_xcorr_register(int ndet, int nrows, const float *p0, const float *p180, int kmax,
+                       int64_t *corr, int *k_best, double *k_sub)
 {
     int nk = 2 * kmax + 1;
+    orc_i128 *c = (orc_i128 *)malloc(sizeof(orc_i128) * (size_t)nk);
+    int bad = 0;
     for (int i = 0; i < nk; ++i) {
         int k = i - kmax;
-        int64_t acc = 0;
+        orc_i128 acc = 0;
         for (int y = 0; y < nrows; ++y)
             for (int x = 0; x < ndet; ++x) {
                 int xm = ndet - 1 - x + k;
                 if (xm < 0 || xm >= ndet) continue;
-                acc += fx_prod(p0[(size_t)y * ndet + x], p180[(size_t)y * ndet + xm]);
+                double p = (double)p0[(size_t)y * ndet + x] * (double)p180[(size_t)y * ndet + xm];
+                if (fabs(p) < 2147483648.0) acc += (orc_i128)(int64_t)floor(p * 4294967296.0);
+                else bad = 1;
             }
-        corr[i] = acc;
+        c[i] = acc;
+    }
+    if (bad) {
+        free(c);
+        return 1;
     }
     int bi = 0;
     for (int i = 1; i < nk; ++i)
-        if (corr[i] > corr[bi]) bi = i;
+        if (c[i] > c[bi]) bi = i;
+    int rc = 0;
+    for (int i = 0; i < nk; ++i) {
+        if (c[i] < (orc_i128)INT64_MIN || c[i] > (orc_i128)INT64_MAX) rc = 2;
+        if (corr) corr[i] = (int64_t)c[i];
+    }
     *k_best = bi - kmax;
     double frac = 0.0;
     if (bi > 0 && bi < nk - 1) {
-        double cm = (double)corr[bi - 1], c0 = (double)corr[bi], cp = (double)corr[bi + 1];
+        double cm = i128_to_double(c[bi - 1]), c0 = i128_to_double(c[bi]), cp = i128_to_double(c[bi + 1]);
         double den = cm - 2.0 * c0 + cp;
         if (den < 0.0) frac = 0.5 * (cm - cp) / den;
     }
     *k_sub = (double)(bi - kmax) + frac;
+    free(c);
+    return rc;
 }
 
 /* ====================================================================== */

@@ -64,6 +64,7 @@ def lib():
         L.orc_proj_to_sino.argtypes = [_c_int, _c_int, _c_int, _f32p, _c_float, _c_float, _f32p]
         L.orc_xcorr_register.argtypes = [_c_int, _c_int, _f32p, _f32p, _c_int, _i64p,
                                          ctypes.POINTER(_c_int), ctypes.POINTER(_c_double)]
+        L.orc_xcorr_register.restype = _c_int
         L.orc_tv_loss_grad_f64.argtypes = [_c_int, _c_int, _f32p, _f64p, _f64p, _f64p, _c_double,
                                            _c_double, ctypes.c_void_p, ctypes.c_void_p]
         L.orc_tv_loss_grad_f64.restype = _c_double
@@ -221,11 +222,21 @@ def proj_to_sino(proj, theta, shift):
 
 
 def xcorr_register(p0, p180, kmax):
+    """Returns (k_best, k_sub, corr); raises ValueError for input whose
+    products are out of the fixed-point range (not finite, or >= 2^31), and
+    OverflowError when a sum does not fit int64 (k_best and k_sub are then
+    attached to the exception as .k_best / .k_sub)."""
     a, b = _c(p0, np.float32), _c(p180, np.float32)
     nrows, ndet = a.shape
     corr = np.empty(2 * kmax + 1, np.int64)
     kb, ks = _c_int(), _c_double()
-    lib().orc_xcorr_register(ndet, nrows, a, b, kmax, corr, ctypes.byref(kb), ctypes.byref(ks))
+    rc = lib().orc_xcorr_register(ndet, nrows, a, b, kmax, corr, ctypes.byref(kb), ctypes.byref(ks))
+    if rc == 1:
+        raise ValueError("projection value not finite, or |p0*p180| >= 2^31")
+    if rc == 2:
+        e = OverflowError("a correlation sum exceeds int64")
+        e.k_best, e.k_sub = kb.value, ks.value
+        raise e
     return kb.value, ks.value, corr
 
 

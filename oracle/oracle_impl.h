@@ -15,6 +15,15 @@
 #error "REAL must be defined"
 #endif
 
+/* floor() of a coordinate as an int, without a libm call: truncate, then
+ * step down for negative non-integers.  Equal to (int)floor(x) wherever the
+ * result fits an int, which every grid coordinate here does.              */
+static inline int SFX(ifloor)(REAL x)
+{
+    int i = (int)x;
+    return i - ((REAL)i > x);
+}
+
 /* tomography/tv_hpc.F90:53-56 -- filter taps, jx = 1..2N+1 */
 void SFX(orc_filter_taps)(int N, REAL *filt)
 {
@@ -112,7 +121,7 @@ void SFX(orc_backproject)(int N, int T, const float *theta, int wpu, int S,
             REAL sum = R(0.0);
             for (int t = 0; t < T; ++t) {
                 REAL yr = (sb[t] * ((REAL)jx - mid) + cb[t] * ((REAL)jy - mid)) + mid;
-                int y1 = (int)RFLOOR(yr);
+                int y1 = SFX(ifloor)(yr);
                 int y2 = y1 + 1;
                 if (y1 > 1 && y2 < N + 1) {
                     const REAL *qt = q + (size_t)t * N;
@@ -153,8 +162,8 @@ void SFX(orc_radon)(int N, int T, const float *theta, int S, const REAL *img, RE
             for (int jx = 1; jx <= N; ++jx) {
                 REAL xr = (c * ((REAL)jx - mid) - sn * ((REAL)jy - mid)) + mid;
                 REAL yr = (sn * ((REAL)jx - mid) + c * ((REAL)jy - mid)) + mid;
-                int y1 = (int)RFLOOR(yr), y2 = y1 + 1;
-                int x1 = (int)RFLOOR(xr), x2 = x1 + 1;
+                int y1 = SFX(ifloor)(yr), y2 = y1 + 1;
+                int x1 = SFX(ifloor)(xr), x2 = x1 + 1;
                 int mn = x1 < y1 ? x1 : y1, mx = x2 > y2 ? x2 : y2;
                 if (mn > 1 && mx < N + 1) {
                     REAL a = u[(size_t)(y1 - 1) * N + (x1 - 1)];
@@ -192,8 +201,8 @@ void SFX(orc_radon_adjoint)(int N, int T, const float *theta, int S, const REAL 
                 for (int jx = 1; jx <= N; ++jx) {
                     REAL xr = (c * ((REAL)jx - mid) - sn * ((REAL)jy - mid)) + mid;
                     REAL yr = (sn * ((REAL)jx - mid) + c * ((REAL)jy - mid)) + mid;
-                    int y1 = (int)RFLOOR(yr), y2 = y1 + 1;
-                    int x1 = (int)RFLOOR(xr), x2 = x1 + 1;
+                    int y1 = SFX(ifloor)(yr), y2 = y1 + 1;
+                    int x1 = SFX(ifloor)(xr), x2 = x1 + 1;
                     int mn = x1 < y1 ? x1 : y1, mx = x2 > y2 ? x2 : y2;
                     if (mn > 1 && mx < N + 1) {
                         REAL wxl = (REAL)x2 - xr, wxh = xr - (REAL)x1;

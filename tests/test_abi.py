@@ -70,3 +70,20 @@ def test_binding_constants_match_the_header():
     fparams = {k: int(v) for k, v in re.findall(r"(ACU_\w+)\s*=\s*(-?\d+)", f90)}
     for k, v in consts.items():
         assert fparams.get(k) == v, k
+
+
+def test_noalloc_registration_rejects_bad_arguments_without_gpu(built_lib):
+    """acu_xcorr_register_noalloc checks its arguments before any CUDA call:
+    the lag range of its fixed scratch (1..2048), the frame shape and the
+    pointers.  The device pointers below are never dereferenced."""
+    from acumen_gb300 import _lib
+    L = _lib.lib()
+    fake = ctypes.c_void_p(0x1000)
+    kb, ks = ctypes.c_int(), ctypes.c_double()
+    for ndet, nrows, kmax, p0, pk in ((64, 4, 0, fake, ctypes.byref(kb)), (64, 4, 2049, fake, ctypes.byref(kb)),
+                                      (1, 4, 8, fake, ctypes.byref(kb)), (64, 0, 8, fake, ctypes.byref(kb)),
+                                      (64, 4, 8, None, ctypes.byref(kb)), (64, 4, 8, fake, None)):
+        rc = L.acu_xcorr_register_noalloc(ndet, nrows, p0, fake, kmax, None, pk, ctypes.byref(ks), None)
+        assert rc == _lib.ACU_ERR_INVALID
+    rc = L.acu_xcorr_register_noalloc(64, 4, fake, fake, 2049, None, ctypes.byref(kb), ctypes.byref(ks), None)
+    assert b"outside 1..2048" in L.acu_last_error(None)

@@ -106,10 +106,13 @@ def test_pipeline_through_drivers(dataset, oracle):
     for pipe in ("1", "0"):
         run("fbp_hpc", dict(env, ACUMEN_BATCH="10", ACUMEN_PIPELINE=pipe))
         np.testing.assert_array_equal(read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N), fbp)
-    # ACUMEN_POSITIONS=exact selects the exact sample positions; a bad value fails
+    # exact sample positions are the default (ACUMEN_POSITIONS=exact gives the same files);
+    # ACUMEN_POSITIONS=reference selects the reference's single-precision arithmetic; a bad value fails
     run("fbp_hpc", dict(env, ACUMEN_POSITIONS="exact"))
-    fbpx = read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N)
-    assert rel(fbpx, ref_fbp64) < 1e-5 and not np.array_equal(fbpx, fbp)
+    np.testing.assert_array_equal(read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N), fbp)
+    run("fbp_hpc", dict(env, ACUMEN_POSITIONS="reference"))
+    fbpr = read_split(rec, "fbp", nfr, N * N, NIMG).reshape(NIMG, N, N)
+    assert rel(fbpr, oracle.iradon(f.astype(np.float32), tw, 4, 32)) < 1e-5 and not np.array_equal(fbpr, fbp)
     r = subprocess.run([os.path.join(B.BIN, "fbp_hpc")], env=dict(env, ACUMEN_POSITIONS="bogus"),
                        capture_output=True, text=True, timeout=600)
     assert r.returncode != 0 and "ACUMEN_POSITIONS" in (r.stdout + r.stderr)

@@ -71,6 +71,7 @@ def test_radon_random_image_full_support(case, oracle):
     N = case["N"]
     x = rng.standard_normal((5, N, N)).astype(np.float32)
     t = Tomography(N, case["th"], case["wpu"])
+    t.set_option(8, 0)                     # the reference's single-precision positions
     got = t.radon(torch.from_numpy(x).cuda())
     assert rel(got, oracle.radon(x, case["th"], 32)) < 1e-6
     inner = x.copy()
@@ -163,6 +164,7 @@ def test_projector_variants_agree(case, oracle):
     taps) compute the same sums up to summation order, also on random images
     that reach the border."""
     t = Tomography(case["N"], case["th"], case["wpu"])
+    t.set_option(8, 0)                     # the reference's single-precision positions
     rng = np.random.default_rng(5)
     for x in (case["img"][:5].astype(np.float32), rng.standard_normal((5, case["N"], case["N"])).astype(np.float32)):
         img = torch.from_numpy(x).cuda()
@@ -181,8 +183,8 @@ def test_projector_variants_agree(case, oracle):
 
 
 def test_exact_positions_backprojection(oracle, built_lib):
-    """Option 8 = 1: backprojection sample positions from the split FP64 angle
-    tables.  On a ramp-filtered-like (high-pass) input at a 1025 grid, where
+    """Option 8 = 1 (the default): backprojection sample positions from the split FP64 angle
+    tables, against option 8 = 0.  On a ramp-filtered-like (high-pass) input at a 1025 grid, where
     the reference's single-precision positions are off by ~6e-5 px, the exact
     positions bring the result to single-precision round-off of the FP64
     oracle."""
@@ -191,6 +193,8 @@ def test_exact_positions_backprojection(oracle, built_lib):
     q = np.random.default_rng(11).standard_normal((1, T, N)).astype(np.float32)
     ref64 = oracle.backproject(q.astype(np.float64), th, wpu, 64)
     t = Tomography(N, th, wpu)
+    assert t.get_option(8) == 1            # exact positions are the default
+    t.set_option(8, 0)
     qc = torch.from_numpy(q).cuda()
     e_ref = rel(t.backproject(qc), ref64)
     t.set_option(8, 1)
@@ -213,6 +217,7 @@ def test_exact_positions_projector_and_adjoint(oracle, built_lib):
     x[:, :3, :] = x[:, -3:, :] = x[:, :, :3] = x[:, :, -3:] = 0
     ref64 = oracle.radon(x.astype(np.float64), th, 64)
     t = Tomography(N, th, wpu)
+    t.set_option(8, 0)
     xc = torch.from_numpy(x).cuda()
     e_ref = rel(t.radon(xc), ref64)
     t.set_option(8, 1)

@@ -112,6 +112,38 @@ def test_registration_matches_oracle_and_truth(pp, oracle, stack):
     assert ks == pytest.approx(kso, abs=1e-12)
 
 
+def test_xcorr_rejects_nonfinite_input(pp):
+    from acumen_gb300._lib import ACU_ERR_INVALID, AcumenError
+    p0 = np.ones((4, 16), np.float32)
+    p180 = np.ones((4, 16), np.float32)
+    for bad in (np.nan, np.inf):
+        q0 = p0.copy()
+        q0[1, 7] = bad
+        with pytest.raises(AcumenError, match="not finite") as ei:
+            pp.xcorr_register(cu(q0), cu(p180), 3)
+        assert ei.value.code == ACU_ERR_INVALID
+    kb, ks, corr = pp.xcorr_register(cu(p0), cu(p180), 3)     # the context stays usable
+    assert kb == 0
+
+
+def test_xcorr_sums_beyond_int64(pp, oracle):
+    """Sums beyond 2^63 are exact in 128 bits: the lag matches the oracle's;
+    corr_out, which is int64, is refused for them."""
+    from acumen_gb300._lib import ACU_ERR_UNSUPPORTED, AcumenError
+    rng = np.random.default_rng(22)
+    p0 = rng.uniform(30000, 40000, (40, 64)).astype(np.float32)
+    p180 = (np.roll(np.ascontiguousarray(p0[:, ::-1]), 3, axis=1) * np.float32(0.9)).astype(np.float32)
+    with pytest.raises(OverflowError) as ei:
+        oracle.xcorr_register(p0, p180, 5)
+    with pytest.raises(AcumenError) as eg:
+        pp.xcorr_register(cu(p0), cu(p180), 5)
+    assert eg.value.code == ACU_ERR_UNSUPPORTED
+    kb, ks, corr = pp.xcorr_register(cu(p0), cu(p180), 5, want_corr=False)
+    assert corr is None
+    assert kb == ei.value.k_best
+    assert ks == ei.value.k_sub
+
+
 @pytest.mark.parametrize("reg", [0, 1])
 def test_full_chain_host_buffers(pp, oracle, stack, reg):
     sino, th, sh = pp.proj_to_sino_u16(stack["raw"], stack["th"], stack["flats"], stack["darks"], norm_mode=1,

@@ -228,3 +228,53 @@ def test_register_recovers_axis_offset(oracle, offset):
     k_true = 2 * (axis_true - 1) - (ndet - 1)
     assert abs(k - k_true) <= 1
     assert abs(ksub - k_true) < 0.5
+
+
+def _xcorr_exact(p0, p180, kmax):
+    """The correlation sums with Python integers: floor(p0*p180*2^32) summed
+    without bound (float64 products of two float32 values are exact)."""
+    nrows, ndet = p0.shape
+    a, b = p0.astype(np.float64), p180.astype(np.float64)
+    out = []
+    for k in range(-kmax, kmax + 1):
+        s = 0
+        for x in range(ndet):
+            xm = ndet - 1 - x + k
+            if 0 <= xm < ndet:
+                s += sum(int(np.floor(v)) for v in a[:, x] * b[:, xm] * 4294967296.0)
+        out.append(s)
+    return out
+
+
+def test_xcorr_sums_are_exact_integers(oracle):
+    rng = np.random.default_rng(21)
+    p0 = rng.uniform(-3, 3, (5, 23)).astype(np.float32)
+    p180 = rng.uniform(-3, 3, (5, 23)).astype(np.float32)
+    k, ksub, corr = oracle.xcorr_register(p0, p180, 6)
+    ref = _xcorr_exact(p0, p180, 6)
+    assert corr.tolist() == ref
+    assert k == int(np.argmax(ref)) - 6
+
+
+def test_xcorr_rejects_nonfinite_and_out_of_range_products(oracle):
+    p0 = np.ones((4, 16), np.float32)
+    p180 = np.ones((4, 16), np.float32)
+    for bad in (np.nan, np.inf, 5e4):          # 5e4 * 1 is fine alone; 5e4^2 >= 2^31
+        q0, q180 = p0.copy(), p180.copy()
+        q0[2, 5] = bad
+        q180[2, 16 - 1 - 5] = bad if bad == 5e4 else 1.0
+        with pytest.raises(ValueError):
+            oracle.xcorr_register(q0, q180, 3)
+
+
+def test_xcorr_sums_beyond_int64_keep_the_exact_argmax(oracle):
+    # products ~1.2e9 (below 2^31) over 40 x 64 pixels: sums ~1.3e22 > 2^63
+    rng = np.random.default_rng(22)
+    p0 = rng.uniform(30000, 40000, (40, 64)).astype(np.float32)
+    p180 = np.ascontiguousarray(p0[:, ::-1])
+    p180 = np.roll(p180, 3, axis=1) * np.float32(0.9)
+    with pytest.raises(OverflowError) as ei:
+        oracle.xcorr_register(p0, p180, 5)
+    ref = _xcorr_exact(p0, p180, 5)
+    assert max(abs(v) for v in ref) > 2 ** 63
+    assert ei.value.k_best == int(np.argmax(ref)) - 5

@@ -55,6 +55,23 @@ def test_noalloc_matches_context_entry_point_twice(built_lib):
     pp.close()
 
 
+def test_noalloc_call_leaves_device_memory_unchanged(built_lib):
+    """After a first call (which may load the library's device code), further
+    calls allocate nothing: the device's free memory is the same before and
+    after, and torch's allocator saw no new allocation."""
+    p0, p180 = _pair(6, 1.5)
+    _noalloc(p0, p180, 2048)                  # warm-up: the largest lag range
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    alloc0 = torch.cuda.memory_stats().get("allocation.all.allocated", 0)
+    for kmax in (2048, 7):
+        _noalloc(p0, p180, kmax)
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    assert free1 == free0
+    assert torch.cuda.memory_stats().get("allocation.all.allocated", 0) == alloc0
+
+
 def test_noalloc_rejects_lag_range_beyond_scratch(built_lib):
     p0, p180 = _pair(5, 0.0)
     with pytest.raises(_lib.AcumenError, match="outside 1..2048"):
