@@ -89,7 +89,24 @@ def build_drivers(force: bool = False) -> list:
     return out
 
 
+PROBE = os.path.join(BIN, "l1_peak")
+
+
+def build_probe(force: bool = False) -> str:
+    """The L1 load-bandwidth probe (csrc/l1_peak.cu), a standalone program that
+    bench.py runs for the measured ceiling of the gather kernels."""
+    src = os.path.join(CSRC, "l1_peak.cu")
+    os.makedirs(BIN, exist_ok=True)
+    if force or not os.path.exists(PROBE) or os.path.getmtime(PROBE) < os.path.getmtime(src):
+        r = subprocess.run([nvcc(), *ARCH, "-O3", "-lineinfo", "-std=c++17", src, "-o", PROBE],
+                           capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"probe build failed:\n{r.stderr}")
+    return PROBE
+
+
 if __name__ == "__main__":
     build(force="--force" in sys.argv, verbose_ptxas="-v" in sys.argv)
     build_drivers(force="--force" in sys.argv)
+    build_probe(force="--force" in sys.argv)
     print(OUT)

@@ -200,62 +200,128 @@ def job_value(world, slices_per_rank, t_warm, t_step):
 
 
 # ---------------------------------------------------------------------------
-def cpu_reference_sample(N, T, threads=None, t_sample=24, nslices=None):
-    """The reference's algorithm on the host cores: the oracle's single-precision
-    radon + iradon (direct filter) of `nslices` slices (one per core, as the
-    reference's MPI ranks) on `t_sample` of the T angles.  Returns seconds of
-    one radon+iradon pair for that sample and the sample description."""
+def _cpu_slice(N, T, seed=1000):
+    """One seeded synthetic sinogram of the workload (the first slice of the batch)."""
     import numpy as np
-    from oracle import oracle as O
     from acumen_gb300 import synthetic as syn
-    ncores = threads or os.cpu_count() or 1
-    ns = nslices or ncores
-    th = syn.angles(T, closed=True)[:: max(1, T // t_sample)][:t_sample]
-    rng = np.random.default_rng(0)
-    img = rng.random((ns, N, N), dtype=np.float32)
-    sino = rng.random((ns, len(th), N), dtype=np.float32)
+    th = syn.angles(T, closed=True)
+    f = syn.normalised_sinogram(syn.random_ellipses(seed, 0.35 * N), N, th, I0=5e3, seed=seed).numpy()
+    return th, np.ascontiguousarray(f, np.float32)
+
+
+def cpu_outer_iteration(N, T):
+    """The reference's algorithm on the host cores, measured: the oracle's
+    single-precision restatement of tomography/tv_hpc.F90:162-363 (source
+    operation order, single-precision reductions, direct filter) on one
+    full-size slice, OpenMP over every host core inside each operator.  Times
+    the FBP warm start (one iradon) and one complete Bregman outer iteration
+    (orc_tvopt with nouter = 1 minus its warm start: the right-hand side, the
+    initial residual, ncg CG steps, the shrinkage and the Bregman update).
+    slices/s = 1 / (t_warm + nouter * t_outer): only the iteration count is
+    scaled."""
+    from oracle import oracle as O
+    ncores = os.cpu_count() or 1
+    th, f = _cpu_slice(N, T)
     O.lib()
     t0 = time.perf_counter()
-    O.radon(img, th, 32)
-    t1 = time.perf_counter()
-    O.iradon(sino, th, WPU, 32)
-    t2 = time.perf_counter()
-    desc = (f"oracle single-precision radon + iradon (direct filter) of {ns} slices of {N}^2 on "
-            f"{len(th)} of {T} angles, OpenMP over {ncores} threads; scaled by T/{len(th)} and by "
-            f"the reference's {NCG + 2} radon + {NCG + 2} iradon per outer iteration")
-    return (t1 - t0), (t2 - t1), len(th), ns, ncores, desc
-
-
-def cpu_slices_per_s(N, T, threads=None):
-    tr, ti, ts, ns, ncores, desc = cpu_reference_sample(N, T, threads)
-    scale = T / ts
-    t_outer = (NCG + 2) * (tr + ti) * scale          # ns slices in parallel
-    t_job = NOUTER * t_outer + ti * scale           # + FBP warm start
-    return ns / t_job, ncores, desc
+    O.iradon(f, th, WPU, 32)
+    t_warm = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    O.tvopt(f, th, WPU, NINNER, 1, NCG, LAM, MU, prec=32, red_mode=0)
+    t_one = time.perf_counter() - t0
+    t_outer = max(t_one - t_warm, 1e-9)
+    desc = (f"oracle single-precision tvopt (tv_hpc.F90:162-363) of one {N}^2 slice at {T} angles with nouter=1 "
+            f"(ninner={NINNER}, ncg={NCG}): warm start {t_warm:.2f} s + one outer iteration {t_outer:.2f} s, "
+            f"OpenMP over {ncores} threads inside each operator; slices/s = 1/(t_warm + {NOUTER} t_outer)")
+    return 1.0 / (t_warm + NOUTER * t_outer), ncores, desc, t_warm, t_outer
 
 
 # ---------------------------------------------------------------------------
-def l1_level(achieved_gbps, clocks, **extra):
-    """The gather kernels run from L2 and L1, so their bound is the L1 data path:
-    128 bytes per clock per SM (nominal, Blackwell) x SMs x the SM clock
-    measured during the timed region.  Not a measured peak: labelled nominal."""
+# ---------------------------------------------------------------------------
+def measure_l1_peak():
+    """The measured L1 load bandwidth: acumen_gb300/bin/l1_peak (csrc/l1_peak.cu),
+    128-bit loads over an L1-resident buffer on every SM.  None if the probe
+    cannot run."""
+    from acumen_gb300 import build as _build
+    try:
+        exe = _build.build_probe()
+        r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+        d = json.loads(r.stdout.strip().splitlines()[-1])
+        return d if "l1_gbps" in d else None
+    except Exception:
+        return None
+
+
+def l1_level(achieved_gbps, clocks, probe=None, **extra):
+    """The gather kernels run from L2 and L1, so their bound is the L1 data path.
+    Peak: the probe's measured L1 load bandwidth, scaled from the probe's own SM
+    clock to the median SM clock of the timed region; without the probe, the
+    nominal 128 bytes per clock per SM."""
     import torch
     sms = torch.cuda.get_device_properties(0).multi_processor_count
     mhz = clocks.get("sm_mhz") or clocks.get("sm_max_mhz") or 2070.0
-    peak = 128.0 * sms * mhz * 1e6 / 1e9
-    out = {"achieved_GBps": achieved_gbps, "peak_GBps": peak, "frac": achieved_gbps / peak,
-           "peak_kind": f"nominal: 128 B/clk/SM x {sms} SMs x {mhz:.0f} MHz"}
+    if probe:
+        scale = mhz / probe["sm_mhz_from_cycles"] if probe.get("sm_mhz_from_cycles") else 1.0
+        peak = probe["l1_gbps"] * scale
+        kind = (f"measured: {probe['l1_gbps']:.0f} GB/s = {probe['bytes_per_clk_per_sm']:.1f} B/clk/SM at "
+                f"{probe['sm_mhz_from_cycles']:.0f} MHz (bin/l1_peak), scaled to {mhz:.0f} MHz")
+    else:
+        peak = 128.0 * sms * mhz * 1e6 / 1e9
+        kind = f"nominal: 128 B/clk/SM x {sms} SMs x {mhz:.0f} MHz"
+    out = {"achieved_GBps": achieved_gbps, "peak_GBps": peak, "frac": achieved_gbps / peak, "peak_kind": kind}
     out.update(extra)
     return out
 
 
+GOLDEN_TV = os.path.join(ROOT, "tests", "golden", "tv_1449sq_900ang.npz")
+
+
+def tv_golden():
+    """TV at 1449^2 x 900 angles, 50 x 10 (lambda 0.05, mu 1), against the
+    committed golden results of the CPU oracle in FP64 and in the reference's
+    single precision (tests/golden/make_golden.py), both position modes, the
+    batched and the plain per-slice path; relative L2 inside the
+    reconstruction disc and over the full image."""
+    import numpy as np
+    import torch
+    from acumen_gb300.tomography import Tomography
+    if not os.path.exists(GOLDEN_TV):
+        return {"missing": GOLDEN_TV}
+    z = np.load(GOLDEN_TV)
+    N, T = int(z["params"][0]), int(z["params"][1])
+    I0 = float(z["params"][2])
+    f = torch.from_numpy((-np.log(z["counts"].astype(np.float64) / max(I0, 1.0))).astype(np.float32))[None].cuda()
+    ref = {"fp64": torch.from_numpy(z["tv_f64"]).cuda(), "fp32": torch.from_numpy(z["tv_f32"]).cuda()}
+    t = Tomography(N, z["theta"], WPU)
+    mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0]
+    rel = lambda a, b, m=None: float(torch.linalg.norm((a.double() - b.double())[..., m] if m is not None else
+                                                       a.double() - b.double()) /
+                                     torch.linalg.norm(b.double()[..., m] if m is not None else b.double()))
+    out = {"grid": N, "angles": T, "iterations": f"{NOUTER} x {NCG}", "reference": "oracle FP64 and FP32 (golden)"}
+    t0 = time.perf_counter()
+    for name, pos in POSITIONS.items():
+        t.set_option(8, pos)
+        for path, plain in (("batched", False), ("plain", True)):
+            tv, _ = t.tvopt(f, NINNER, NOUTER, NCG, LAM, MU, plain=plain)
+            tv = tv[0]
+            out[f"{name}_positions_{path}"] = {
+                "rel_l2_disc_vs_fp64": rel(tv, ref["fp64"], mask), "rel_l2_full_vs_fp64": rel(tv, ref["fp64"]),
+                "rel_l2_disc_vs_fp32_oracle": rel(tv, ref["fp32"], mask),
+                "rel_l2_full_vs_fp32_oracle": rel(tv, ref["fp32"])}
+    out["fp32_oracle_rel_l2_disc_vs_fp64"] = rel(ref["fp32"], ref["fp64"], mask)
+    out["seconds"] = time.perf_counter() - t0
+    t.close()
+    return out
+
+
 def accuracy(full=False):
-    """Errors against FP64 at the configurations' full sizes, for both
-    single-precision position modes (ACU_OPT_POSITIONS).  The FP64 reference
-    here is the library's double-precision solver, itself checked against the
-    FP64 CPU oracle to 1e-9 at test sizes (tests/test_gpu_tv.py).  full=True
-    (bench.py --op accuracy) adds one slice of the 2049^2 x 1200 workload and
-    the plain per-slice path; the FP64 solves take minutes there."""
+    """Errors at the configurations' full sizes for both single-precision
+    position modes (ACU_OPT_POSITIONS): TV against the committed golden
+    results of the CPU oracle (tv_golden), FBP against the library's
+    double-precision path (itself checked against the FP64 CPU oracle to 1e-11
+    at test sizes, tests/test_gpu_ops.py).  full=True (bench.py --op accuracy)
+    adds a second 1449^2 phantom and one slice of the 2049^2 x 1200 workload
+    against the library's FP64 solver; the FP64 solves take minutes there."""
     import torch
     from acumen_gb300 import synthetic as syn
     from acumen_gb300.tomography import Tomography
@@ -287,8 +353,9 @@ def accuracy(full=False):
         res["seconds"] = time.perf_counter() - t0
         return res
 
-    out = {"tv_1449sq_900ang": tv_case(1449, 900, 2, full)}      # single slice, 1448 bins made odd
+    out = {"tv_1449sq_900ang_golden": tv_golden()}
     if full:
+        out["tv_1449sq_900ang"] = tv_case(1449, 900, 2, True)      # single slice, 1448 bins made odd
         out["tv_2049sq_1200ang_one_slice"] = tv_case(N_GRID, T_ANG, 3, False)
     # FBP of one 725^2 slice at 720 angles from Poisson counts
     N, T = 725, 720
@@ -371,20 +438,43 @@ def uneven_batch(nprob=64, seed=7, positions=1):
 
 
 def run_reference(args, rank, world):
+    """The reference arm: the reference's algorithm on the host cores (the
+    oracle's single-precision restatement; the reference is Fortran and has no
+    compiler here).  A step is one CG step of the inner solve
+    (tomography/tv_hpc.F90:253-300: radon(p), iradon, the operator's Laplacian
+    term, the inner products and the vector updates) on one full-size slice,
+    OpenMP over every host core.  An outer iteration of the reference holds
+    ncg + 2 such radon + iradon pairs (tv_hpc.F90:227-229 right-hand side and
+    initial residual, :253-254 the CG steps, :339-340 the Bregman update), so
+    slices/s = 1 / (nouter * (ncg + 2) * t_step)."""
     if rank != 0:
         return
-    vals = []
-    for i in range(args.warmup + args.steps):
-        v, ncores, desc = cpu_slices_per_s(args.size, args.angles)
-        if i >= args.warmup:
-            vals.append(v)
-    v = statistics.median(vals)
+    import numpy as np
+    from oracle import oracle as O
+    from acumen_gb300 import synthetic as syn
+    N, T = args.size, args.angles
+    ncores = os.cpu_count() or 1
+    th = syn.angles(T, closed=True)
+    cg = O.CGState(N, th, WPU, LAM, MU, prec=32, red_mode=0)
+    for _ in range(args.warmup):
+        cg.step()
+    ts = []
+    for _ in range(args.steps):
+        t0 = time.perf_counter()
+        cg.step()
+        ts.append(time.perf_counter() - t0)
+    t_step = statistics.mean(ts)
+    v = 1.0 / (NOUTER * (NCG + 2) * t_step)
+    desc = (f"oracle single-precision CG step (tv_hpc.F90:253-300: radon, iradon with the direct filter, "
+            f"Laplacian, inner products, updates) of one {N}^2 slice at {T} angles, OpenMP over {ncores} threads; "
+            f"slices/s = 1/({NOUTER} outer x {NCG + 2} radon+iradon pairs x t_step)")
     line = {"metric": METRIC, "value": v, "unit": "slices/s", "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1000.0 * args.slices / v / NOUTER, "higher_is_better": True,
+            "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "impl": "reference",
-            "config": {"workload": f"split-Bregman TV, {args.slices} slices of {args.size}^2, {args.angles} angles, "
-                                   f"ninner={NINNER} ncg={NCG} nouter={NOUTER} lambda={LAM} mu={MU} wpu={WPU}",
+            "config": {"workload": f"split-Bregman TV, {args.slices} slices of {N}^2, {T} angles, "
+                                   f"ninner={NINNER} ncg={NCG} nouter={NOUTER} lambda={LAM} mu={MU} wpu={WPU}; "
+                                   f"step = one CG step of one slice",
                        "global_batch": args.slices, "parallelism": "host threads"},
             "cpu_baseline": {"value": v, "unit": "slices/s", "cores": ncores, "kind": "port", "sample": desc},
             "e2e": {"value": v, "unit": "slices/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -497,6 +587,26 @@ def main():
             "clocks": clocks, "gpu_launches": kernel_launches}
 
     if rank == 0 and not args.no_extras:
+        # the same solver in the reference's order of operations: the initial CG
+        # residual from two backprojections (ACU_OPT_RESIDUAL = 0) and radon(uk)
+        # recomputed after every outer iteration (ACU_OPT_RADON_REFRESH = 1):
+        # (ncg + 2) projections and (ncg + 2) filtered backprojections per step,
+        # the work of the plain per-slice path
+        opt9, opt11 = t.get_option(9), t.get_option(11)
+        t.set_option(9, 0)
+        t.set_option(11, 1)
+        t_warm_eq = cuda_time(lambda: t.tv_begin(f, NINNER, NCG, LAM, MU), 1)
+        t.tv_iterate(1)
+        t_step_eq = cuda_time(lambda: t.tv_iterate(1), 2)
+        t.set_option(9, opt9)
+        t.set_option(11, opt11)
+        equal = {"value": S / (t_warm_eq + NOUTER * t_step_eq), "unit": "slices/s", "t_step_s": t_step_eq,
+                 "t_warm_s": t_warm_eq,
+                 "options": "ACU_OPT_RESIDUAL=0, ACU_OPT_RADON_REFRESH=1: the reference's order "
+                            "(tv_hpc.F90:227-229, 253-254, 339-340), 12 projections + 12 filtered "
+                            "backprojections per outer iteration"}
+        probe = measure_l1_peak()
+        line["l1_probe"] = probe
         # dominant kernel: the projector, timed alone on the same batch (lane layout, 64 slice groups)
         img = torch.rand(S, N, N, device="cuda")
         t_radon = cuda_time(lambda: t.radon(img), 2)
@@ -517,7 +627,7 @@ def main():
                             "note": "runs from L2 and L1, not from HBM (each band of rows stays in L2); traffic (from "
                                     "one 32-slice ncu capture, scaled by 32-slice line groups) is mostly the ray "
                                     "sums carried between the band launches, ~1.4 % of the HBM bandwidth",
-                            "l1_level": l1_level(16.0 * N * N * T * S / t_radon / 1e9, clocks,
+                            "l1_level": l1_level(16.0 * N * N * T * S / t_radon / 1e9, clocks, probe,
                                                  bytes_per_sample_slice=16,
                                                  sample_slices_per_s=N * N * T * S / t_radon)}
         # end to end through the host-buffer C ABI: one outer iteration with copies
@@ -546,8 +656,11 @@ def main():
         tp2 = cuda_time(lambda: t.tvopt(f1, NINNER, 2, NCG, LAM, MU, plain=True), 1)
         t_plain_outer = max(tp2 - tp1, 1e-9)
         plain_val = 1.0 / (tp1 - t_plain_outer + NOUTER * t_plain_outer)
+        equal["batched_over_plain"] = equal["value"] / plain_val
         line["plain_gpu"] = {"value": plain_val, "unit": "slices/s", "outer_s_per_slice": t_plain_outer,
-                             "batched_over_plain": value / plain_val}
+                             "batched_over_plain": value / plain_val,
+                             "batched_over_plain_equal_work": equal["batched_over_plain"]}
+        line["equal_work"] = equal
         # FBP GUPS: one 725^2 slice at 720 angles, and the batch
         from acumen_gb300 import synthetic as syn
         t1c = Tomography(725, syn.angles(720), WPU)
@@ -563,7 +676,7 @@ def main():
         line["roofline_backprojection"] = {
             "kernel": "k_backproject_exact_ct<4, 1> (tv_hpc.F90:107-123)", "launch_ms": 1000 * t_bp,
             "updates_per_s": N * N * T * S / t_bp,
-            "l1_level": l1_level(8.0 * N * N * T * S / t_bp / 1e9, clocks, bytes_per_update=8),
+            "l1_level": l1_level(8.0 * N * N * T * S / t_bp / 1e9, clocks, probe, bytes_per_update=8),
             "note": "neighbouring pixels' taps often fall in the same bins and are broadcast within a "
                     "quarter-warp, so bytes delivered to registers can exceed the data path's 128 B/clk; "
                     "ncu: 80 % of L1 data-pipe wavefronts and 80 % issue; launch includes the lane-layout "
@@ -575,8 +688,8 @@ def main():
         line["uneven_batch"] = uneven_batch(positions=POSITIONS[args.positions])
         line["pipeline"] = pipeline()
         line["accuracy"] = accuracy()
-        # CPU baseline (bounded sample, all host cores)
-        v, ncores, desc = cpu_slices_per_s(N, T)
+        # CPU baseline (one measured outer iteration of one slice, all host cores)
+        v, ncores, desc, _, _ = cpu_outer_iteration(N, T)
         line["cpu_baseline"] = {"value": v, "unit": "slices/s", "cores": ncores, "kind": "port", "sample": desc}
     if rank == 0:
         print(json.dumps(line), flush=True)

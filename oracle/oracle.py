@@ -51,6 +51,9 @@ def lib():
             getattr(L, f"orc_tvopt_{sfx}").argtypes = [_c_int, _c_int, _f32p, _c_int, _c_int, p,
                                                        _c_int, _c_int, _c_int, real, real, _c_int, p,
                                                        ctypes.c_void_p]
+            getattr(L, f"orc_cg_step_{sfx}").argtypes = [_c_int, _c_int, _f32p, _c_int, real, real, _c_int,
+                                                         p, p, p, p, p, p, _c_double]
+            getattr(L, f"orc_cg_step_{sfx}").restype = _c_double
         L.orc_frame_average.argtypes = [_c_int, _c_long, _f32p, _f32p]
         L.orc_normalize.argtypes = [_c_int, _c_long, _f32p, _f32p, _f32p, _f32p]
         L.orc_minloc_abs.argtypes = [_c_int, _f32p, _c_float]
@@ -159,6 +162,30 @@ def tvopt(f, theta, wpu, ninner, nouter, ncg, lam, mu, prec=64, red_mode=1):
     getattr(lib(), f"orc_tvopt_{s}")(N, T, _c(theta, np.float32), wpu, S, x, ninner, nouter, ncg,
                                      lam, mu, red_mode, tv, fbp.ctypes.data_as(ctypes.c_void_p))
     return tv, fbp
+
+
+class CGState:
+    """Work arrays of one slice's inner CG solve (tomography/tv_hpc.F90:253-300)
+    for timing single CG steps: uk, r, p, Ap, irpt (N*N) and rp (T*N)."""
+
+    def __init__(self, N, theta, wpu, lam, mu, prec=32, red_mode=0, seed=0):
+        dt, self._s = _dt(prec)
+        rng = np.random.default_rng(seed)
+        self.N, self.theta, self.wpu = N, _c(theta, np.float32), wpu
+        self.lam, self.mu, self.red = lam, mu, red_mode
+        self.uk = np.zeros((N, N), dt)
+        self.r = _c(rng.standard_normal((N, N)), dt)
+        self.p = self.r.copy()
+        self.Ap = np.empty((N, N), dt)
+        self.irpt = np.empty((N, N), dt)
+        self.rp = np.empty((len(theta), N), dt)
+        self.rsold = float(np.sum(self.r.astype(np.float64) ** 2))
+
+    def step(self):
+        self.rsold = getattr(lib(), f"orc_cg_step_{self._s}")(
+            self.N, len(self.theta), self.theta, self.wpu, self.lam, self.mu, self.red, self.uk, self.r, self.p,
+            self.Ap, self.rp, self.irpt, self.rsold)
+        return self.rsold
 
 
 def frame_average(frames):

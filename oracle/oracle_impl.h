@@ -249,6 +249,42 @@ static double SFX(sum_dot)(int N, const REAL *a, const REAL *b, int red_mode)
     return s;
 }
 
+/* tomography/tv_hpc.F90:253-300 -- one CG step of the inner solve on
+ * M = mu*iradon(radon(.)) + lambda*(periodic Laplacian): rp = radon(p),
+ * irpt = iradon(rp), Ap, alpha = rsold/<p,Ap>, uk += alpha p, r -= alpha Ap,
+ * beta = rsnew/rsold, p = r + beta p.  Returns rsnew.  Work arrays: Ap, irpt
+ * (N*N) and rp (N*T).                                                       */
+double SFX(orc_cg_step)(int N, int T, const float *theta, int wpu, REAL lambda, REAL mu, int red_mode,
+                        REAL *uk, REAL *r, REAL *p, REAL *Ap, REAL *rp, REAL *irpt, double rsold)
+{
+    size_t NN = (size_t)N * N;
+#define AT(a, x, y) (a)[(size_t)((y) - 1) * N + ((x) - 1)]
+    SFX(orc_radon)(N, T, theta, 1, p, rp);
+    SFX(orc_iradon)(N, T, theta, wpu, 1, rp, irpt);
+    for (int jy = 1; jy <= N; ++jy)
+        for (int jx = 1; jx <= N; ++jx) {
+            int jxr = SFX(nb_next)(jx, N), jyr = SFX(nb_next)(jy, N);
+            int jxl = SFX(nb_prev)(jx, N), jyl = SFX(nb_prev)(jy, N);
+            REAL lap = (((R(4.0) * AT(p, jx, jy) - AT(p, jxl, jy)) - AT(p, jxr, jy)) - AT(p, jx, jyl)) - AT(p, jx, jyr);
+            AT(Ap, jx, jy) = mu * AT(irpt, jx, jy) + lambda * lap;
+        }
+#undef AT
+    double num = SFX(sum_dot)(N, p, Ap, red_mode);
+    REAL alpha;
+    if (red_mode == 0 && sizeof(REAL) == sizeof(float)) alpha = (REAL)((float)rsold / (float)num);
+    else alpha = (REAL)(rsold / num);
+    for (size_t i = 0; i < NN; ++i) {
+        uk[i] = uk[i] + alpha * p[i];
+        r[i] = r[i] - alpha * Ap[i];
+    }
+    double rsnew = SFX(sum_sq)(N, r, red_mode);
+    REAL beta;
+    if (red_mode == 0 && sizeof(REAL) == sizeof(float)) beta = (REAL)((float)rsnew / (float)rsold);
+    else beta = (REAL)(rsnew / rsold);
+    for (size_t i = 0; i < NN; ++i) p[i] = r[i] + beta * p[i];
+    return rsnew;
+}
+
 /* tomography/tv_hpc.F90:162-363 -- split-Bregman TV with an inner CG solve,
  * one slice.  Outputs the FBP warm start (fbp) and the TV result (tv).
  * err_log (optional, nouter entries) receives the print-only Err_diff.   */
@@ -302,35 +338,8 @@ static void SFX(tvopt_one)(int N, int T, const float *theta, int wpu,
                     AT(p, jx, jy) = AT(r, jx, jy);
                 }
             double rsold = SFX(sum_sq)(N, r, red_mode);
-            for (int jncg = 1; jncg <= ncg; ++jncg) {
-                SFX(orc_radon)(N, T, theta, 1, p, rp);
-                SFX(orc_iradon)(N, T, theta, wpu, 1, rp, irpt);
-                for (int jy = 1; jy <= N; ++jy)
-                    for (int jx = 1; jx <= N; ++jx) {
-                        int jxr = SFX(nb_next)(jx, N), jyr = SFX(nb_next)(jy, N);
-                        int jxl = SFX(nb_prev)(jx, N), jyl = SFX(nb_prev)(jy, N);
-                        REAL lap = (((R(4.0) * AT(p, jx, jy) - AT(p, jxl, jy)) - AT(p, jxr, jy)) - AT(p, jx, jyl)) - AT(p, jx, jyr);
-                        AT(Ap, jx, jy) = mu * AT(irpt, jx, jy) + lambda * lap;
-                    }
-                double num = SFX(sum_dot)(N, p, Ap, red_mode);
-                REAL alpha;
-                double rsnew;
-                if (red_mode == 0 && sizeof(REAL) == sizeof(float)) {
-                    alpha = (REAL)((float)rsold / (float)num);
-                } else {
-                    alpha = (REAL)(rsold / num);
-                }
-                for (size_t i = 0; i < NN; ++i) {
-                    uk[i] = uk[i] + alpha * p[i];
-                    r[i] = r[i] - alpha * Ap[i];
-                }
-                rsnew = SFX(sum_sq)(N, r, red_mode);
-                REAL beta;
-                if (red_mode == 0 && sizeof(REAL) == sizeof(float)) beta = (REAL)((float)rsnew / (float)rsold);
-                else beta = (REAL)(rsnew / rsold);
-                for (size_t i = 0; i < NN; ++i) p[i] = r[i] + beta * p[i];
-                rsold = rsnew;
-            }
+            for (int jncg = 1; jncg <= ncg; ++jncg)
+                rsold = SFX(orc_cg_step)(N, T, theta, wpu, lambda, mu, red_mode, uk, r, p, Ap, rp, irpt, rsold);
             const REAL thr = R(1.0) / lambda;
             for (int jy = 1; jy <= N; ++jy)
                 for (int jx = 1; jx <= N; ++jx) {

@@ -12,16 +12,21 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 TINY = ["--impl", "reference", "--size", "65", "--angles", "24", "--slices", "4", "--steps", "2", "--warmup", "1"]
 
 
-def run_bench(extra_env=None):
+def run_bench(extra_env=None, wall=None):
+    import time
     env = dict(os.environ, **(extra_env or {}))
+    t0 = time.perf_counter()
     r = subprocess.run([sys.executable, os.path.join(ROOT, "bench.py"), *TINY], env=env, capture_output=True,
                        text=True, timeout=600, cwd=ROOT)
+    if wall is not None:
+        wall.append(time.perf_counter() - t0)
     assert r.returncode == 0, r.stderr[-2000:]
     return [l for l in r.stdout.splitlines() if l.startswith("{")]
 
 
 def test_reference_arm_line(oracle):
-    lines = run_bench()
+    wall = []
+    lines = run_bench(wall=wall)
     assert len(lines) == 1
     d = json.loads(lines[0])
     for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
@@ -34,6 +39,19 @@ def test_reference_arm_line(oracle):
     e = d["e2e"]
     assert e["value"] == d["value"] and e["unit"] == d["unit"]
     assert e["h2d_bytes_per_step"] == 0 and e["d2h_bytes_per_step"] == 0
+    # the steps are measured, not modelled: their time fits inside the run
+    assert d["steps"] * d["ms_per_step"] / 1000.0 < wall[0]
+    # slices/s of the full reconstruction from the measured CG step
+    assert abs(d["value"] * 50 * 12 * d["ms_per_step"] / 1000.0 - 1.0) < 1e-9
+
+
+def test_cpu_baseline_times_a_full_outer_iteration(oracle):
+    sys.path.insert(0, ROOT)
+    import bench
+    v, cores, desc, t_warm, t_outer = bench.cpu_outer_iteration(65, 24)
+    assert v > 0 and cores >= 1 and t_warm > 0 and t_outer > 0
+    assert abs(v * (t_warm + 50 * t_outer) - 1.0) < 1e-9
+    assert "nouter=1" in desc
 
 
 def test_reference_arm_other_ranks_print_nothing(oracle):
