@@ -8,6 +8,7 @@
 // Arithmetic that decides an index or a comparison is written with explicit
 // round-to-nearest operations so that it matches the single-precision
 // reference operation for operation.
+#include <algorithm>
 #include <climits>
 #include <cmath>
 
@@ -47,6 +48,56 @@ __global__ void k_normalize(int mode, long npix, long total, const Tin* __restri
             v = -logf(__fdiv_rn(fmaxf(__fsub_rn(I, d), 1e-16f), fmaxf(__fsub_rn(ob[k], d), 1.0f)));
         }
         out[i] = v;
+    }
+}
+
+// Vectorised form for frames of a multiple of 8 pixels with 16-byte aligned
+// arrays: one thread normalises 8 consecutive pixels of one projection (a
+// 16-byte load of uint16 counts or two of floats, two 16-byte loads of each
+// flat/dark average, two 16-byte stores); grid.y walks the projections, so no
+// 64-bit division is needed.  Same arithmetic per pixel as k_normalize.
+__device__ __forceinline__ void load8(const uint16_t* p, float (&v)[8])
+{
+    const uint4 u = __ldg(reinterpret_cast<const uint4*>(p));
+    const unsigned w[4] = {u.x, u.y, u.z, u.w};
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+        v[2 * i] = (float)(w[i] & 0xffffu);
+        v[2 * i + 1] = (float)(w[i] >> 16);
+    }
+}
+__device__ __forceinline__ void load8(const float* p, float (&v)[8])
+{
+    const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+    v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w;
+    v[4] = b.x; v[5] = b.y; v[6] = b.z; v[7] = b.w;
+}
+
+template <typename Tin>
+__global__ void __launch_bounds__(256) k_normalize8(int mode, int nproj, long nvec, const Tin* __restrict__ raw,
+                                                    const float* __restrict__ ob, const float* __restrict__ df,
+                                                    float* __restrict__ out)
+{
+    for (int p = blockIdx.y; p < nproj; p += gridDim.y) {
+        const Tin* rp = raw + (size_t)p * nvec * 8;
+        float* op = out + (size_t)p * nvec * 8;
+        for (long v = blockIdx.x * (long)blockDim.x + threadIdx.x; v < nvec; v += (long)gridDim.x * blockDim.x) {
+            float I[8], o[8], d[8];
+            load8(rp + v * 8, I);
+            load8(ob + v * 8, o);
+            if (mode == 0) {
+#pragma unroll
+                for (int i = 0; i < 8; ++i) I[i] = -logf(__fdiv_rn(I[i], fmaxf(o[i], 1.0f)));
+            } else {
+                load8(df + v * 8, d);
+#pragma unroll
+                for (int i = 0; i < 8; ++i)
+                    I[i] = -logf(__fdiv_rn(fmaxf(__fsub_rn(I[i], d[i]), 1e-16f), fmaxf(__fsub_rn(o[i], d[i]), 1.0f)));
+            }
+            float4* q = reinterpret_cast<float4*>(op + v * 8);
+            q[0] = make_float4(I[0], I[1], I[2], I[3]);
+            q[1] = make_float4(I[4], I[5], I[6], I[7]);
+        }
     }
 }
 
@@ -248,6 +299,73 @@ __global__ void k_argmax(int nk, unsigned long long* __restrict__ w)
 // ---- 27-point median (:426-452): the reference's descending exchange sort,
 // passes 1..14 (the later passes do not touch element 14), with the
 // intended slots 1..27 ------------------------------------------------------------
+// When the 27 values hold no NaN and no zero, every selection of the 14th
+// largest returns the same bits (equal finite non-zero floats, and equal
+// infinities, are bitwise equal), so a cheaper selection is used: forgetful
+// selection, which keeps 15 candidates, moves their minimum and maximum to the
+// ends with compare-exchanges (min/max pairs), drops both, takes in the next
+// value and repeats -- 390 min/max operations instead of the 273
+// compare-and-swap steps (819 instructions) of the exchange sort.  With a NaN
+// (whose comparisons are false) or a signed zero present, the exchange sort
+// itself decides, bit for bit.
+__device__ __forceinline__ void cx_minmax(float& a, float& b)
+{
+    const float lo = fminf(a, b), hi = fmaxf(a, b);
+    a = lo;
+    b = hi;
+}
+
+__device__ __forceinline__ float median27_select(float (&r)[27])
+{
+    bool plain = true;
+#pragma unroll
+    for (int i = 0; i < 27; ++i) plain &= fabsf(r[i]) > 0.0f;   // false for NaN and +-0
+    if (plain) {
+#pragma unroll
+        for (int A = 0; A <= 12; ++A) {
+#pragma unroll
+            for (int i = A + 1; i <= 14; ++i) cx_minmax(r[A], r[i]);   // minimum of r[A..14] to r[A]
+#pragma unroll
+            for (int i = A + 1; i < 14; ++i) cx_minmax(r[i], r[14]);   // maximum to r[14]
+            if (A < 12) r[14] = r[15 + A];                               // drop both, take the next
+        }
+        return r[13];
+    }
+#pragma unroll
+    for (int a = 0; a < 14; ++a) {
+        float ra = r[a];
+#pragma unroll
+        for (int b = a + 1; b < 27; ++b) {
+            const float rb = r[b];
+            const bool sw = rb > ra;
+            r[b] = sw ? ra : rb;
+            ra = sw ? rb : ra;
+        }
+        r[a] = ra;
+    }
+    return r[13];
+}
+
+// The median at (jx, jy) (1-based) of the 3x3 neighbourhood, clamped to the
+// frame, in the previous (dl), current (dc) and next (dr) projection.
+__device__ __forceinline__ float median27_at(const float* __restrict__ dl, const float* __restrict__ dc,
+                                             const float* __restrict__ dr, int ndet, int nrows, int jx, int jy)
+{
+    float r[27];
+#pragma unroll
+    for (int jxs = -1; jxs <= 1; ++jxs)
+#pragma unroll
+        for (int jys = -1; jys <= 1; ++jys) {
+            const int cx = min(max(jx + jxs, 1), ndet), cy = min(max(jy + jys, 1), nrows);
+            const size_t o = (size_t)(cy - 1) * ndet + (cx - 1);
+            const int slot = 3 * (jxs + 1) + (jys + 1);
+            r[slot] = __ldg(dl + o);
+            r[slot + 9] = __ldg(dc + o);
+            r[slot + 18] = __ldg(dr + o);
+        }
+    return median27_select(r);
+}
+
 __global__ void __launch_bounds__(128) k_median27(int ndet, int nrows, int nproj_chunk, int p_first, int nfiles,
                                                   const float* __restrict__ proj, float* __restrict__ out)
 {
@@ -261,31 +379,7 @@ __global__ void __launch_bounds__(128) k_median27(int ndet, int nrows, int nproj
         const float* dc = proj + (size_t)p * npix;
         const float* dl = p > 0 ? dc - npix : dc;
         const float* dr = p < nfiles - 1 ? dc + npix : dc;
-        float r[27];
-#pragma unroll
-        for (int jxs = -1; jxs <= 1; ++jxs)
-#pragma unroll
-            for (int jys = -1; jys <= 1; ++jys) {
-                const int cx = min(max(jx + jxs, 1), ndet), cy = min(max(jy + jys, 1), nrows);
-                const size_t o = (size_t)(cy - 1) * ndet + (cx - 1);
-                const int slot = 3 * (jxs + 1) + (jys + 1);
-                r[slot] = __ldg(dl + o);
-                r[slot + 9] = __ldg(dc + o);
-                r[slot + 18] = __ldg(dr + o);
-            }
-#pragma unroll
-        for (int a = 0; a < 14; ++a) {
-            float ra = r[a];
-#pragma unroll
-            for (int b = a + 1; b < 27; ++b) {
-                const float rb = r[b];
-                const bool sw = rb > ra;
-                r[b] = sw ? ra : rb;
-                ra = sw ? rb : ra;
-            }
-            r[a] = ra;
-        }
-        out[(size_t)pc * npix + k] = r[13];
+        out[(size_t)pc * npix + k] = median27_at(dl, dc, dr, ndet, nrows, jx, jy);
     }
 }
 
@@ -322,17 +416,30 @@ void launch_frame_average_f32(int nf, long npix, const float* f, float* out, cud
 {
     k_frame_average<float><<<nblocks(npix, 256), 256, 0, st>>>(nf, npix, f, out);
 }
+static bool aligned16(const void* p) { return ((uintptr_t)p & 15u) == 0; }
+
+template <typename Tin>
+static void launch_normalize(int mode, int nproj, long npix, const Tin* raw, const float* ob, const float* df,
+                             float* out, cudaStream_t st)
+{
+    if (npix % 8 == 0 && aligned16(raw) && aligned16(ob) && aligned16(out) && (mode == 0 || aligned16(df))) {
+        const long nvec = npix / 8;
+        dim3 grd(nblocks(nvec, 256, 2048), (unsigned)std::min(nproj, 32768));
+        k_normalize8<Tin><<<grd, 256, 0, st>>>(mode, nproj, nvec, raw, ob, df, out);
+    } else {
+        const long total = npix * nproj;
+        k_normalize<Tin><<<nblocks(total, 256), 256, 0, st>>>(mode, npix, total, raw, ob, df, out);
+    }
+}
 void launch_normalize_u16(int mode, int nproj, long npix, const uint16_t* raw, const float* ob, const float* df,
                           float* out, cudaStream_t st)
 {
-    const long total = npix * nproj;
-    k_normalize<uint16_t><<<nblocks(total, 256), 256, 0, st>>>(mode, npix, total, raw, ob, df, out);
+    launch_normalize<uint16_t>(mode, nproj, npix, raw, ob, df, out, st);
 }
 void launch_normalize_f32(int mode, int nproj, long npix, const float* raw, const float* ob, const float* df,
                           float* out, cudaStream_t st)
 {
-    const long total = npix * nproj;
-    k_normalize<float><<<nblocks(total, 256), 256, 0, st>>>(mode, npix, total, raw, ob, df, out);
+    launch_normalize<float>(mode, nproj, npix, raw, ob, df, out, st);
 }
 void launch_lerp(long n, const float* a, const float* b, float ta, float tb, float target, float* out,
                  cudaStream_t st)

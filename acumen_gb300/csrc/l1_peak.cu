@@ -1,11 +1,13 @@
 // L1 load-bandwidth probe: the measured ceiling of the gather kernels
 // (the projector and the backprojection run from L1 and L2, not from HBM).
 //
-// Every block reads the same 16 KB buffer over and over with 128-bit
-// non-coherent loads (ld.global.nc.v4.f32): after the first pass it sits in
-// each SM's L1, so the loop measures the L1 data path alone.  A warp's load
-// covers 512 consecutive bytes, four aligned 128-byte lines, the access
-// pattern of the pixel-line projector.  Reports bytes per second over all
+// Every block reads the same 64 KB buffer over and over with 128-bit
+// non-coherent loads (ld.global.nc.v4.f32, volatile inline PTX, so the
+// compiler can neither merge nor hoist them): after the first pass the buffer
+// sits in each SM's L1, so the loop measures the L1 data path alone.  A warp's
+// load covers 512 consecutive bytes, four aligned 128-byte lines, the access
+// pattern of the pixel-line projector; the eight loads of an iteration and
+// consecutive iterations touch different lines.  Reports bytes per second over all
 // SMs, bytes per SM clock (the clock taken from the SM's own cycle counter
 // over the timed kernel) and that clock.  Prints one JSON line.
 //
@@ -18,34 +20,42 @@
 
 namespace {
 
-constexpr int kWords = 1024;        // float4 words in the buffer: 16 KB
+constexpr int kWords = 4096;        // float4 words in the buffer: 64 KB
 constexpr int kThreads = 256;
 constexpr int kUnroll = 8;
+
+__device__ __forceinline__ float4 ld_nc_v4(const float4* p)
+{
+    float4 v;
+    asm volatile("ld.global.nc.v4.f32 {%0, %1, %2, %3}, [%4];"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(p));
+    return v;
+}
 
 __global__ void __launch_bounds__(kThreads, 4) k_l1_read(const float4* __restrict__ buf, int reps, float* out,
                                                       long long* cycles)
 {
     const long long c0 = clock64();
-    float4 a[kUnroll];
+    float a[kUnroll];
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) a[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+    for (int u = 0; u < kUnroll; ++u) a[u] = 0.f;
     // thread t starts at word t and strides by the block, so each warp reads
-    // 32 consecutive words (512 bytes) per load; indices wrap inside 16 KB
+    // 32 consecutive words (512 bytes) per load; indices wrap inside 64 KB,
+    // and an iteration advances by 8 x 256 words, half the buffer
     int idx = threadIdx.x;
+#pragma unroll 1
     for (int r = 0; r < reps; ++r) {
+        float4 v[kUnroll];
 #pragma unroll
-        for (int u = 0; u < kUnroll; ++u) {
-            const float4 v = __ldg(buf + ((idx + u * kThreads) & (kWords - 1)));
-            a[u].x += v.x;
-            a[u].y += v.y;
-            a[u].z += v.z;
-            a[u].w += v.w;
-        }
+        for (int u = 0; u < kUnroll; ++u) v[u] = ld_nc_v4(buf + ((idx + u * kThreads) & (kWords - 1)));
+#pragma unroll
+        for (int u = 0; u < kUnroll; ++u) a[u] += (v[u].x + v[u].w) + (v[u].y + v[u].z);
         idx = (idx + kUnroll * kThreads) & (kWords - 1);
     }
     float s = 0.f;
 #pragma unroll
-    for (int u = 0; u < kUnroll; ++u) s += a[u].x + a[u].y + a[u].z + a[u].w;
+    for (int u = 0; u < kUnroll; ++u) s += a[u];
     out[blockIdx.x * blockDim.x + threadIdx.x] = s;
     const long long c1 = clock64();
     if (threadIdx.x == 0) cycles[blockIdx.x] = c1 - c0;
@@ -106,7 +116,7 @@ int main()
     const double mhz = best_cyc / (best_ms * 1e-3) / 1e6;
     const double per_clk_sm = bytes / sms / best_cyc;
     std::printf("{\"l1_gbps\": %.1f, \"bytes_per_clk_per_sm\": %.2f, \"sm_mhz_from_cycles\": %.0f, \"sms\": %d, "
-                "\"ms\": %.3f, \"bytes\": %.0f, \"how\": \"ld.global.nc.v4.f32 over a 16 KB L1-resident buffer, "
+                "\"ms\": %.3f, \"bytes\": %.0f, \"how\": \"ld.global.nc.v4.f32 over a 64 KB L1-resident buffer, "
                 "%d blocks x %d threads, %d x %d loads per thread, best of 10, CUDA events\"}\n",
                 gbps, per_clk_sm, mhz, sms, best_ms, bytes, nblk, kThreads, reps, kUnroll);
     cudaFree(buf);

@@ -80,7 +80,14 @@ void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& ou
         const double pid = 4.0 * std::atan(1.0);
         out.xsc_bp.resize(4 * (size_t)T);
         out.xsc_fp.resize(4 * (size_t)T);
+        // A sine or cosine below 1e-12 is the FP64 rounding residue of a
+        // grid-aligned angle (cos(pi/2) evaluates to 6.1e-17): its true value
+        // is 0.  Kept, it would move samples that lie exactly on a cell edge
+        // by ~1e-15 px to the other side of the edge, where the FP64
+        // evaluation rounds them back onto it; at the grid border that flips
+        // the validity test (tv_hpc.F90:117,149) against FP64.
         auto split = [&](double v, float& a, float& r) {
+            if (std::fabs(v) < 1e-12) v = 0.0;
             const double av = std::ldexp(std::nearbyint(std::ldexp(v, out.xq)), -out.xq);
             a = (float)av;
             r = (float)(v - av);

@@ -405,11 +405,107 @@ def pipeline(nproj=1200, ndet=2048, nrows=256, seed=3):
     return out
 
 
-def uneven_batch(nprob=64, seed=7, positions=1):
+def pipeline_device(nproj=1200, ndet=2048, nrows=256, seed=3, acc_outer=3):
+    """Config 3 end to end in HBM: 1200 uint16 projections of 2048 x 256 with
+    10 flat and 10 dark frames and a random rotation-axis offset in [-8, 8] px
+    -> frame averages -> normalisation (mode 1) -> 0/180-degree picks ->
+    cross-correlation registration -> median, resample and transpose to 256
+    sinograms of 1200 x 2049 -> batched TV on those sinograms.  Each stage is
+    timed on the device (CUDA events, inputs resident); the HBM fraction of
+    the streaming stages is their compulsory bytes over their time against the
+    measured copy bandwidth.  slices/s = S / (t_prep + t_warm + nouter t_step)
+    with the TV warm start and steps timed on the pipeline's own sinograms;
+    accuracy: slice nrows/2 after acc_outer outer iterations against the
+    library's double-precision solver on that slice."""
+    import numpy as np
+    import torch
+    from acumen_gb300 import synthetic as syn
+    from acumen_gb300.preprocess import Preprocessor
+    from acumen_gb300.tomography import Tomography
+    hbm, kind = measured_peaks()
+    rng = np.random.default_rng(seed)
+    offset = float(rng.uniform(-8, 8))
+    th, raw, flats, darks = syn.projection_stack(nproj, ndet, nrows, offset, seed, device="cuda")
+    bits = lambda x: x.to(torch.int32).to(torch.int16).contiguous()   # the uint16 counts' bit pattern
+    raw, flats, darks = bits(raw), bits(flats), bits(darks)
+    pp = Preprocessor()
+    npix = ndet * nrows
+    add = 1 if ndet % 2 == 0 else 0
+    res = {"shape": [nproj, nrows, ndet], "offset_px": offset, "input": "uint16 + 10 flat + 10 dark, in HBM"}
+
+    def timed(fn, reps=3):
+        fn()
+        return cuda_time(fn, reps)
+
+    t_avg = timed(lambda: (pp.frame_average(flats), pp.frame_average(darks)))
+    ob, df = pp.frame_average(flats), pp.frame_average(darks)
+    t_norm = timed(lambda: pp.normalize(raw, ob, df, 1))
+    proj = pp.normalize(raw, ob, df, 1)
+    t_pick = timed(lambda: (pp.pick_angle(th, proj, 0.0), pp.pick_angle(th, proj, 180.0)))
+    p0, p180 = pp.pick_angle(th, proj, 0.0), pp.pick_angle(th, proj, 180.0)
+    kmax = max(1, min(ndet // 4, 512))
+    t_reg = timed(lambda: pp.xcorr_register(p0, p180, kmax, want_corr=False))
+    kb, ks, _ = pp.xcorr_register(p0, p180, kmax, want_corr=False)
+    shift = (add - ks) / (2.0 * ndet)
+    t_mrt = timed(lambda: pp.proj_to_sino(proj, 0.0, shift), 2)
+    sino = pp.proj_to_sino(proj, 0.0, shift)
+    del proj
+    nx = ndet + add
+    stages = {
+        "frame_average": {"ms": 1e3 * t_avg, "bytes": 2 * 20 * npix + 2 * 4 * npix},
+        "normalize": {"ms": 1e3 * t_norm, "bytes": nproj * npix * (2 + 4) + 2 * 4 * npix},
+        "pick_0_180": {"ms": 1e3 * t_pick, "bytes": 2 * (2 * 4 * npix + 4 * npix)},
+        "xcorr_register": {"ms": 1e3 * t_reg, "bytes": 2 * 4 * npix, "kmax": kmax},
+        "median_resample_transpose": {"ms": 1e3 * t_mrt, "bytes": nproj * npix * 4 + nproj * nrows * nx * 4},
+    }
+    for v in stages.values():
+        v["GBps"] = v["bytes"] / (v["ms"] * 1e-3) / 1e9
+        v["hbm_frac"] = v["GBps"] / hbm
+    res["stages"] = stages
+    t_prep = (t_avg + t_norm + t_pick + t_reg + t_mrt)
+    res["prep_device_s"] = t_prep
+    add_axis = (nx + 1) / 2 - shift * ndet
+    res["axis_error_px"] = add_axis - ((nx + 1) // 2 + offset)
+    del raw
+    torch.cuda.empty_cache()
+    # batched TV on the pipeline's sinograms: f[slice][angle][bin]
+    t = Tomography(nx, th, WPU)
+    t_warm = cuda_time(lambda: t.tv_begin(sino, NINNER, NCG, LAM, MU), 1)
+    t.tv_iterate(1)
+    t_step = cuda_time(lambda: t.tv_iterate(1), 2)
+    S = nrows
+    res.update({"tv_warm_s": t_warm, "tv_step_s": t_step,
+                "value": S / (t_prep + t_warm + NOUTER * t_step), "unit": "slices/s",
+                "how": "S / (device preprocessing + TV warm start + 50 x TV step), TV batched in exact positions"})
+    # accuracy of one slice of the chain's output against FP64 at acc_outer outer iterations
+    k = S // 2
+    f1 = sino[k:k + 1].contiguous()
+    tv32, _ = t.tvopt(f1, NINNER, acc_outer, NCG, LAM, MU)
+    tv64, _ = t.tvopt(f1.double(), NINNER, acc_outer, NCG, LAM, MU)
+    mask = (t.backproject(torch.ones(1, nproj, nx, device="cuda")) != 0)[0]
+    a, b = tv32[0].double()[mask], tv64[0][mask]
+    res["rel_l2_disc_vs_fp64"] = float(torch.linalg.norm(a - b) / torch.linalg.norm(b))
+    res["accuracy_how"] = f"slice {k}, {acc_outer} outer x {NCG} CG iterations, FP32 batched vs the FP64 solver"
+    t.close()
+    pp.close()
+    del sino
+    torch.cuda.empty_cache()
+    return res
+
+
+def uneven_batch(nprob=64, seed=7, positions=1, acc_outer=1):
+    """Config 4: 64 independent problems with sides drawn from {256, 512, 1024,
+    1536, 2048} (grid = ceil(sqrt(2) side), made odd) and 180-1500 angles, one
+    ragged batch (acu_batch_tvopt).  Throughput from t(nouter=1) and
+    t(nouter=6); accuracy: every problem's single-precision batched result
+    after acc_outer outer iterations (x ncg CG steps) against the library's
+    double-precision solver on that problem alone, relative L2 inside the
+    reconstruction disc."""
     import numpy as np
     import torch
     from acumen_gb300 import synthetic as syn
     from acumen_gb300.batch import RaggedBatch
+    from acumen_gb300.tomography import Tomography
     rng = np.random.default_rng(seed)
     sides = rng.choice([256, 512, 1024, 1536, 2048], nprob)
     Ns = [int(np.ceil(np.sqrt(2) * sd)) | 1 for sd in sides]
@@ -421,7 +517,7 @@ def uneven_batch(nprob=64, seed=7, positions=1):
     b.set_option(8, positions)
     b.tvopt(sinos, NINNER, 1, NCG, LAM, MU)             # tuning, graph capture
     t0 = time.perf_counter()
-    b.tvopt(sinos, NINNER, 1, NCG, LAM, MU)
+    tv1, _ = b.tvopt(sinos, NINNER, 1, NCG, LAM, MU)
     t1 = time.perf_counter() - t0
     t0 = time.perf_counter()
     b.tvopt(sinos, NINNER, 6, NCG, LAM, MU)          # outer iterations 2..6: one radon(uk) refresh period
@@ -430,11 +526,101 @@ def uneven_batch(nprob=64, seed=7, positions=1):
     t_job = t1 + (NOUTER - 1) * t_outer
     w, r = b.tuning()
     b.close()
+    tv_acc = tv1 if acc_outer == 1 else None
+    if tv_acc is None:
+        b = RaggedBatch(Ns, ths, WPU)
+        b.set_option(8, positions)
+        tv_acc, _ = b.tvopt(sinos, NINNER, acc_outer, NCG, LAM, MU)
+        b.close()
+    t0 = time.perf_counter()
+    errs = []
+    for N, th, f, tvb in zip(Ns, ths, sinos, tv_acc):
+        t = Tomography(N, th, WPU)
+        mask = (t.backproject(torch.ones(1, len(th), N, device="cuda")) != 0)[0]
+        tv64, _ = t.tvopt(torch.from_numpy(f[None]).double().cuda(), NINNER, acc_outer, NCG, LAM, MU)
+        a, ref = torch.from_numpy(tvb).cuda().double()[mask], tv64[0][mask]
+        errs.append(float(torch.linalg.norm(a - ref) / torch.linalg.norm(ref)))
+        t.close()
     return {"value": nprob / t_job, "unit": "problems/s", "problems": nprob, "outer_s": t_outer,
             "grid_sides": sorted(set(Ns)), "angles": [min(Ts), max(Ts)],
             "samples_per_outer": float(sum((NCG + 1) * T * N * N for N, T in zip(Ns, Ts))),
             "tuned": {"radon_warps": w, "bp_rows": r},
-            "how": "host-buffer acu_batch_tvopt; t(nouter=1) + 49 x [t(nouter=6) - t(nouter=1)] / 5"}
+            "how": "host-buffer acu_batch_tvopt; t(nouter=1) + 49 x [t(nouter=6) - t(nouter=1)] / 5",
+            "rel_l2_max": max(errs), "rel_l2_median": statistics.median(errs),
+            "rel_l2_per_problem": errs,
+            "accuracy_how": f"single-precision ragged batch after {acc_outer} outer x {NCG} CG iterations against "
+                            f"the library's FP64 solver on each problem alone, inside the disc "
+                            f"({time.perf_counter() - t0:.0f} s of FP64 solves)"}
+
+
+def gradient_config5(S=32, N=N_GRID, T=1500, seed=11):
+    """Config 5: the registration-aware TV objective
+    1/2 |A_s u - y|^2 + lambda TV_eps(u) and its gradient with respect to the
+    image and to per-angle detector offsets s ~ N(0, 2 px), for 32 slices of
+    2049^2 at 1500 angles (acu_tv_loss_grad_dev).  Reports the time of one
+    loss + gradient of the batch, the device memory the call holds, the
+    single-precision gradient of slice 0 against the double-precision kernels,
+    and central finite differences (h = 1e-3) of the double-precision loss
+    against its analytic gradient at a few image coordinates and offsets."""
+    import numpy as np
+    import torch
+    from acumen_gb300 import synthetic as syn
+    from acumen_gb300.tomography import Tomography
+    LAMG, EPS = 0.05, 0.05
+    th = syn.angles(T)
+    rng = np.random.default_rng(seed)
+    u = torch.empty(S, N, N, device="cuda")
+    y = torch.empty(S, T, N, device="cuda")
+    for s in range(S):
+        ell = syn.random_ellipses(seed + s, 0.35 * N)
+        u[s] = syn.rasterize(ell, N, device="cuda").float()
+        y[s] = syn.analytic_sinogram(ell, N, th, device="cuda").float()
+    u += 0.01 * torch.randn(S, N, N, device="cuda", generator=torch.Generator("cuda").manual_seed(seed))
+    off = torch.from_numpy(rng.normal(0.0, 2.0, (S, T))).float().cuda()
+    t = Tomography(N, th, WPU)
+    torch.cuda.synchronize()
+    free0, _ = torch.cuda.mem_get_info()
+    loss, gu, go = t.tv_loss_grad(u, off, y, LAMG, EPS)           # allocates the work buffers
+    torch.cuda.synchronize()
+    free1, _ = torch.cuda.mem_get_info()
+    sec = cuda_time(lambda: t.tv_loss_grad(u, off, y, LAMG, EPS), 2)
+    # slice 0 in double precision: gradient and finite differences
+    u0, off0, y0 = u[:1].double(), off[:1].double(), y[:1].double()
+    l64, gu64, go64 = t.tv_loss_grad(u0, off0, y0, LAMG, EPS)
+    rel = lambda a, b: float(torch.linalg.norm(a.double() - b) / torch.linalg.norm(b))
+    out = {"slices": S, "grid": N, "angles": T, "seconds_loss_and_grad": sec,
+           "slices_per_s": S / sec,
+           "device_bytes_held_by_call": int(free0 - free1),
+           "inputs_bytes": int(4 * (2 * S * N * N + S * T * N + S * T)),
+           "grad_u_f32_rel_l2_vs_f64": rel(gu[:1], gu64), "grad_off_f32_rel_l2_vs_f64": rel(go[:1], go64),
+           "loss_f32_rel_vs_f64": abs(float(loss[0]) - float(l64)) / abs(float(l64))}
+    h = 1e-3
+
+    def f64loss(uu, oo):
+        return float(t.tv_loss_grad(uu, oo, y0, LAMG, EPS, want_grad=False)[0])
+
+    fd_u, fd_o = [], []
+    for _ in range(3):
+        i, j = (int(v) for v in rng.integers(N // 4, 3 * N // 4, 2))
+        up, um = u0.clone(), u0.clone()
+        up[0, i, j] += h
+        um[0, i, j] -= h
+        fd = (f64loss(up, off0) - f64loss(um, off0)) / (2 * h)
+        g = float(gu64[0, i, j])
+        fd_u.append(abs(fd - g) / max(1.0, abs(g)))
+    gscale = float(torch.sqrt(torch.mean(go64 ** 2)))
+    for k in rng.choice(T, 3, replace=False):
+        op, om = off0.clone(), off0.clone()
+        op[0, k] += h
+        om[0, k] -= h
+        fd = (f64loss(u0, op) - f64loss(u0, om)) / (2 * h)
+        fd_o.append(abs(fd - float(go64[0, k])) / gscale)
+    out.update({"fd_u_max_err": max(fd_u), "fd_off_max_err_over_rms": max(fd_o),
+                "fd_how": "central differences h=1e-3 of the FP64 loss of slice 0: image error relative to "
+                          "max(1, |g|); offset error relative to the offset gradient's RMS (the bilinear "
+                          "projector is piecewise smooth in the offsets)"})
+    t.close()
+    return out
 
 
 def run_reference(args, rank, world):
@@ -686,7 +872,9 @@ def main():
         del f
         torch.cuda.empty_cache()
         line["uneven_batch"] = uneven_batch(positions=POSITIONS[args.positions])
+        line["gradient"] = gradient_config5()
         line["pipeline"] = pipeline()
+        line["pipeline_device"] = pipeline_device()
         line["accuracy"] = accuracy()
         # CPU baseline (one measured outer iteration of one slice, all host cores)
         v, ncores, desc, _, _ = cpu_outer_iteration(N, T)

@@ -26,6 +26,8 @@ def fma32(a, b, c):
 
 
 def split(v, q):
+    if abs(v) < 1e-12:          # the FP64 residue of a grid-aligned angle (csrc/tables.cpp)
+        v = 0.0
     a = np.ldexp(np.rint(np.ldexp(v, q)), -q)
     return f32(a), f32(v - a)
 
@@ -153,3 +155,57 @@ def test_band_walk_visits_every_sample_once_in_step_order(N, H):
                     assert blo <= idx.min() and idx.max() <= bhi, (th, jy, b, blo, bhi, idx.min(), idx.max())
                 seen.extend(idx.tolist())
             assert seen == (np.nonzero(ok)[0] + 1).tolist(), (th, jy)
+
+
+@pytest.mark.parametrize("N", [25, 49, 725])
+def test_grid_aligned_angles_keep_fp64_validity(N):
+    """At 0, 90 and 180 degrees one of the FP64 sines/cosines is a rounding
+    residue (6.1e-17 instead of 0).  Samples then sit exactly on cell edges;
+    FP64 rounds the residue's product away at the grid border, so the exact
+    tables hold 0 there.  Every projector sample (tv_hpc.F90:144-149, with
+    detector offsets too) then passes or fails the validity test exactly as in
+    FP64, and valid samples fall in the same cell wherever the FP64 fraction
+    is not on an edge."""
+    mid = (N + 1) // 2
+    k = 0
+    while (1 << k) <= mid:
+        k += 1
+    q = 23 - k
+    for th in (0.0, 90.0, 180.0):
+        ct = np.pi * (float(np.float32(th)) - 90.0) / 180.0        # projector convention
+        sv, cv = np.sin(ct), np.cos(ct)
+        sa, sr = split(sv, q)
+        ca, cr = split(cv, q)
+        # every sample near the grid border (where validity is decided) and
+        # a sparse set of interior samples
+        near = [j for j in range(1, N + 1) if j <= 4 or j >= N - 3 or j % 97 == 0]
+        for o in (0.0, -1.3, 0.7):
+            for jy in range(1, N + 1):
+                dy = f32(jy - mid)
+                for jx in (range(1, N + 1) if jy in near else near):
+                    dx = f32(jx - mid)
+                    # exact mode with a detector offset o (ProjRay<float, true>)
+                    bxl = fma32(-sa, f32(o), fma32(-sr, f32(o), f32(-sr * dy)))
+                    byl = fma32(ca, f32(o), fma32(cr, f32(o), f32(cr * dy)))
+                    cx, fx = exact_coord(ca, -sa, cr, -sr, dx, dy, f32(mid)) if o == 0 else \
+                        _split_floor(fma32(ca, dx, fma32(-sa, dy, f32(mid))), fma32(cr, dx, bxl))
+                    cy, fy = exact_coord(sa, ca, sr, cr, dx, dy, f32(mid)) if o == 0 else \
+                        _split_floor(fma32(sa, dx, fma32(ca, dy, f32(mid))), fma32(sr, dx, byl))
+                    # FP64 in the oracle's operation order
+                    xr = (cv * (jx - mid) - sv * (jy + o - mid)) + mid
+                    yr = (sv * (jx - mid) + cv * (jy + o - mid)) + mid
+                    x1, y1 = int(np.floor(xr)), int(np.floor(yr))
+                    ok64 = min(x1, y1) > 1 and max(x1, y1) + 1 < N + 1
+                    ok32 = min(cx, cy) > 1 and max(cx, cy) + 1 < N + 1
+                    assert ok32 == ok64, (th, o, jx, jy, xr, yr, cx, cy)
+                    if ok64 and 1e-9 < xr - x1 < 1 - 1e-9:
+                        assert cx == x1
+                    if ok64 and 1e-9 < yr - y1 < 1 - 1e-9:
+                        assert cy == y1
+
+
+def _split_floor(hi, lo):
+    fl = np.floor(hi)
+    fr = f32(f32(hi - fl) + lo)
+    f2 = np.floor(fr)
+    return float(fl) + float(f2), float(f32(fr - f2))

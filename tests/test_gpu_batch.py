@@ -103,3 +103,21 @@ def test_batch_radon_refresh(probs, oracle):
         assert rel(tv5[i], tv1[i], mask) < 2e-5, i
     with pytest.raises(Exception):
         b.set_option(11, -1)
+
+
+def test_batch_at_uneven_batch_sizes_vs_fp64_oracle(oracle, built_lib):
+    """Problems of the 64-problem configuration's sizes (sides 256 and 512:
+    grids 363 and 725, the 180-1500 angle range) in one ragged batch, one
+    outer iteration of 10 CG steps, against the FP64 oracle inside the disc."""
+    rng = np.random.default_rng(64)
+    spec = [(363, 1500), (725, 240), (363, 180)]
+    ths = [syn.angles(T) for _, T in spec]
+    sinos = [syn.analytic_sinogram(syn.random_ellipses(80 + i, 0.35 * N), N, th).numpy()
+             + 1e-3 * rng.standard_normal((len(th), N)) for i, ((N, _), th) in enumerate(zip(spec, ths))]
+    b = RaggedBatch([N for N, _ in spec], ths, 100)
+    tv, fbp = b.tvopt(sinos, 1, 1, 10, 0.05, 1.0)
+    for i, ((N, T), th, f) in enumerate(zip(spec, ths, sinos)):
+        ref_tv, ref_fbp = oracle.tvopt(f, th, 100, 1, 1, 10, 0.05, 1.0, prec=64)
+        mask = oracle.cmask(N, T, 100, 64) > 0
+        assert rel(fbp[i], ref_fbp) < 1e-5, i
+        assert rel(tv[i], ref_tv, mask) < 1e-4, i

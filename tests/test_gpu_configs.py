@@ -52,8 +52,8 @@ def crop512(a, N=725):
 def fbp_case(built_lib, oracle):
     th, ell, counts, flat, dark = syn.counts_sinogram_725(seed=1)
     c = counts.numpy().astype(np.float32)
-    ob = np.full(c.shape[1:], flat, np.float32)
-    df = np.full(c.shape[1:], dark, np.float32)
+    ob = np.full(c.shape, flat, np.float32)      # the flat and dark level of every detector reading
+    df = np.full(c.shape, dark, np.float32)
     return dict(th=th, p={m: oracle.normalize(c, ob, df, m) for m in (0, 1)})
 
 

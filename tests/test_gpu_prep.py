@@ -84,6 +84,23 @@ def test_median_with_nan_matches_reference_sort(pp, oracle):
     np.testing.assert_array_equal(got, oracle.median27(a, b, c))
 
 
+def test_median_ties_zeros_and_infinities_bit_exact(pp, oracle):
+    """Values from a small set (heavy ties), with signed zeros, infinities and
+    a few NaN: the fast selection (no NaN, no zero among the 27) and the
+    exchange sort (otherwise) both give the oracle's bits."""
+    rng = np.random.default_rng(3)
+    vals = np.array([1.0, 2.0, -1.5, 0.25, np.inf, -np.inf, 0.0, -0.0], np.float32)
+    for frac_special in (0.0, 0.05, 0.3):
+        a, b, c = (rng.choice(vals[:4], (33, 41)).astype(np.float32) for _ in range(3))
+        for arr in (a, b, c):
+            m = rng.random(arr.shape) < frac_special
+            arr[m] = rng.choice(vals[4:], m.sum())
+        b[5, 7] = np.nan
+        got = pp.median27(cu(a), cu(b), cu(c)).cpu().numpy()
+        ref = oracle.median27(a, b, c)
+        np.testing.assert_array_equal(got.view(np.uint32), ref.view(np.uint32))
+
+
 def test_proj_to_sino_matches_oracle(pp, oracle, stack):
     ob = oracle.frame_average(stack["flats"].astype(np.float32))
     df = oracle.frame_average(stack["darks"].astype(np.float32))
