@@ -148,181 +148,6 @@ __global__ void __launch_bounds__(32 * LINE_WARPS * LINE_NA, 5) k_radon_lines(
     }
 }
 
-// ---- variant 8: the same band walk with the ray geometry shared by the lanes
-// of a quarter-warp.  In variant 6 the eight lanes of a quarter-warp, which
-// hold the same ray, each evaluate the same sample position.  Here lane h
-// evaluates the position of step j0 + h of the quarter's ray -- the cell
-// offset (-1 when the sample is invalid or outside the band) and the two
-// fractional weights -- and the quarter then walks the eight samples in step
-// order, each lane fetching the sample's offset and weights with three
-// shuffles.  Values, taps and summation order are those of variant 6
-// (wxl = 1 - wxh exactly for every valid cell, in both position modes), so
-// the sums are bit-identical.
-constexpr unsigned FULL = 0xffffffffu;
-#ifndef ACU_LINES_SHARED_MINB
-#define ACU_LINES_SHARED_MINB 4   // resident blocks per SM the register budget is sized for
-#endif
-
-template <bool EX, bool COLS>
-__device__ __forceinline__ void line_segment_shared(const float* __restrict__ p0, int N, int lo, int hi, int nch,
-                                                    const ProjRay<float, EX>& ray, float mid, int ylo, int yhi,
-                                                    int q, int h, float (&acc)[4])
-{
-    const size_t RS = (size_t)N * LINE_W;
-    for (int ch = 0; ch < nch; ++ch) {
-        const int jx = lo + ch * 8 + h;
-        int o = -1;
-        float wxh = 0.f, wyh = 0.f;
-        if (jx <= hi) {
-            int x1, y1;
-            float wxl, wyl;
-            ray.at((float)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
-            if (min(x1, y1) > 1 && max(x1, y1) < N && y1 >= ylo && y1 <= yhi) o = (y1 - 1) * N + (x1 - 1);
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int src = (q << 3) | k;
-            const int ok = __shfl_sync(FULL, o, src);
-            const float wx = __shfl_sync(FULL, wxh, src);
-            const float wy = __shfl_sync(FULL, wyh, src);
-            if (ok >= 0) {
-                const float* p = p0 + (size_t)ok * LINE_W;
-                const float4 t00 = ld_line(p), t10 = ld_line(p + LINE_W);
-                const float4 t01 = ld_line(p + RS), t11 = ld_line(p + RS + LINE_W);
-                const float wxl = __fsub_rn(1.f, wx), wyl = __fsub_rn(1.f, wy);
-                const float w11 = wxl * wyl, w21 = wx * wyl, w12 = wxl * wy, w22 = wx * wy;
-                if constexpr (COLS)
-                    add_sample(acc, t00, t01, t10, t11, w11, w12, w21, w22);
-                else
-                    add_sample(acc, t00, t10, t01, t11, w11, w21, w12, w22);
-            }
-        }
-    }
-}
-
-// Variant 9: variant 8 with the taps of the quarter's previous cell kept in
-// registers.  A ray advances along its major axis (x when COLS, else y) in the
-// direction NEG = false (+) or true (-): the pair of taps on the leading side
-// of a cell (column x1+1 for +x, x1 for -x; row y1+1 for +y, y1 for -y) is
-// loaded for every new cell, and the trailing pair is the previous cell's
-// leading pair when the cell moved one step along the major axis (offset +adv),
-// else it is loaded too.  A sample in the previous cell loads nothing.  The
-// taps' values and the order of the multiply-adds are unchanged: identical sums.
-template <bool EX, bool COLS, bool NEG>
-__device__ __forceinline__ void line_segment_reuse(const float* __restrict__ p0, int N, int lo, int hi, int nch,
-                                                   const ProjRay<float, EX>& ray, float mid, int ylo, int yhi,
-                                                   int q, int h, float (&acc)[4])
-{
-    const int RSI = N * LINE_W;                       // one image row of lines, in floats
-    // offsets (floats) of the leading and trailing pairs from the cell's (x1, y1) line
-    constexpr bool LEAD_HI = !NEG;                    // the leading pair is on the high side
-    const int step_off = COLS ? (NEG ? -1 : 1) : (NEG ? -N : N);
-    const int minor = COLS ? RSI : LINE_W;            // the pair's second tap: one row (COLS) or column on
-    const int lead0 = LEAD_HI ? (COLS ? LINE_W : RSI) : 0;
-    const int trail0 = LEAD_HI ? 0 : (COLS ? LINE_W : RSI);
-    float4 la = make_float4(0.f, 0.f, 0.f, 0.f), lb = la, ta = la, tb = la;   // lead pair, trailing pair
-    int prev = -2 * N * N - 8;                        // matches no cell
-    for (int ch = 0; ch < nch; ++ch) {
-        const int jx = lo + ch * 8 + h;
-        int o = -1;
-        float wxh = 0.f, wyh = 0.f;
-        if (jx <= hi) {
-            int x1, y1;
-            float wxl, wyl;
-            ray.at((float)jx - mid, x1, y1, wxl, wxh, wyl, wyh);
-            if (min(x1, y1) > 1 && max(x1, y1) < N && y1 >= ylo && y1 <= yhi) o = (y1 - 1) * N + (x1 - 1);
-        }
-#pragma unroll
-        for (int k = 0; k < 8; ++k) {
-            const int src = (q << 3) | k;
-            const int ok = __shfl_sync(FULL, o, src);
-            const float wx = __shfl_sync(FULL, wxh, src);
-            const float wy = __shfl_sync(FULL, wyh, src);
-            if (ok >= 0) {
-                if (ok != prev) {
-                    const float* p = p0 + (size_t)ok * LINE_W;
-                    if (ok == prev + step_off) {
-                        ta = la;
-                        tb = lb;
-                    } else {
-                        ta = ld_line(p + trail0);
-                        tb = ld_line(p + trail0 + minor);
-                    }
-                    la = ld_line(p + lead0);
-                    lb = ld_line(p + lead0 + minor);
-                    prev = ok;
-                }
-                // (t00, t10, t01, t11) from the pairs: a pair's second tap is one
-                // row on (COLS) or one column on (rows walked)
-                const float4 lo_a = LEAD_HI ? ta : la, lo_b = LEAD_HI ? tb : lb;   // low side pair
-                const float4 hi_a = LEAD_HI ? la : ta, hi_b = LEAD_HI ? lb : tb;   // high side pair
-                const float wxl = __fsub_rn(1.f, wx), wyl = __fsub_rn(1.f, wy);
-                const float w11 = wxl * wyl, w21 = wx * wyl, w12 = wxl * wy, w22 = wx * wy;
-                if constexpr (COLS)   // low pair = column x1: (t00, t01); high = column x1+1: (t10, t11)
-                    add_sample(acc, lo_a, lo_b, hi_a, hi_b, w11, w12, w21, w22);
-                else                  // low pair = row y1: (t00, t10); high = row y1+1: (t01, t11)
-                    add_sample(acc, lo_a, lo_b, hi_a, hi_b, w11, w21, w12, w22);
-            }
-        }
-    }
-}
-
-template <bool EX, bool REUSE>
-__global__ void __launch_bounds__(32 * LINE_WARPS * LINE_NA, ACU_LINES_SHARED_MINB) k_radon_lines_shared(
-    const float* __restrict__ L, float* __restrict__ A, const float* __restrict__ sc, const float4* __restrict__ xsc,
-    const int* __restrict__ order, int nup, int N, int T, float mid, int step, int H, int nb)
-{
-    const int lane = threadIdx.x & 31, q = lane >> 3, h = lane & 7;
-    const int jy = blockIdx.x * (4 * LINE_WARPS) + (threadIdx.y % LINE_WARPS) * 4 + q + 1;
-    const int a0 = threadIdx.y / LINE_WARPS;   // angle slot of this warp's group
-    const size_t sg = blockIdx.z;
-    const float* p0 = L + sg * N * N * LINE_W + h * 4;
-    const bool ray_ok = jy <= N;               // per quarter-warp
-    const int jyc = ray_ok ? jy : N;           // a valid ray for the geometry of idle quarters
-    for (int k = 0; k < LINE_ANGLES / LINE_NA; ++k) {
-        const int ti = blockIdx.y * LINE_ANGLES + k * LINE_NA + a0;   // warp-uniform
-        if (ti >= T) break;
-        const int t = order[ti];
-        const float s = sc[2 * t], c = sc[2 * t + 1];
-        const int b = ti < nup ? step : nb - 1 - step;
-        const int ylo = 2 + b * H, yhi = min(N - 1, 1 + (b + 1) * H);
-        if (ylo > yhi) continue;
-        int lo, hi;
-        valid_steps(s, c, (float)jyc - mid, mid, N, lo, hi);
-        band_steps(s, c, (float)jyc - mid, mid, N, ylo, yhi, lo, hi);
-        if (!ray_ok) hi = lo - 1;
-        const int nmine = hi >= lo ? (hi - lo + 8) / 8 : 0;
-        const int nch = (int)__reduce_max_sync(FULL, (unsigned)nmine);
-        if (nch == 0) continue;
-        float4* ap = reinterpret_cast<float4*>(A + ((sg * T + t) * N + (jyc - 1)) * LINE_W + h * 4);
-        float acc[4] = {0.f, 0.f, 0.f, 0.f};
-        if (nmine > 0) {
-            const float4 a = *ap;
-            acc[0] = a.x;
-            acc[1] = a.y;
-            acc[2] = a.z;
-            acc[3] = a.w;
-        }
-        const ProjRay<float, EX> ray(sc, xsc, t, jyc, mid, nullptr);
-        const bool cols = fabsf(c) > fabsf(s);
-        if constexpr (REUSE) {
-            // the major axis advances with jx by c (COLS: xr) or s (yr)
-            if (cols) {
-                if (c < 0.f) line_segment_reuse<EX, true, true>(p0, N, lo, hi, nch, ray, mid, ylo, yhi, q, h, acc);
-                else line_segment_reuse<EX, true, false>(p0, N, lo, hi, nch, ray, mid, ylo, yhi, q, h, acc);
-            } else {
-                if (s < 0.f) line_segment_reuse<EX, false, true>(p0, N, lo, hi, nch, ray, mid, ylo, yhi, q, h, acc);
-                else line_segment_reuse<EX, false, false>(p0, N, lo, hi, nch, ray, mid, ylo, yhi, q, h, acc);
-            }
-        } else if (cols) {
-            line_segment_shared<EX, true>(p0, N, lo, hi, nch, ray, mid, ylo, yhi, q, h, acc);
-        } else {
-            line_segment_shared<EX, false>(p0, N, lo, hi, nch, ray, mid, ylo, yhi, q, h, acc);
-        }
-        if (nmine > 0) *ap = make_float4(acc[0], acc[1], acc[2], acc[3]);
-    }
-}
-
 // Lane image [G][npix][4] -> line image [SG][npix][8][4]; groups G..8SG-1 are
 // zero.  One thread per 16-byte slot of the output.
 __global__ void k_lines_from_lanes(const float4* __restrict__ img, float4* __restrict__ L, int G, size_t npix,
@@ -366,7 +191,7 @@ size_t lines_image_floats(int N, int G) { return (size_t)((G + 7) / 8) * N * N *
 size_t lines_sums_floats(int N, int T, int G) { return (size_t)((G + 7) / 8) * T * N * LINE_W; }
 
 void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float* L, float* A, float* sino,
-                        cudaStream_t st, int mode)
+                        cudaStream_t st)
 {
     const int N = g.N, T = g.T, SG = (G + 7) / 8;
     if (G <= 0 || N <= 0 || T <= 0) return;
@@ -379,17 +204,12 @@ void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float*
     dim3 blk(32, LINE_WARPS * LINE_NA);
     dim3 grd((N + 4 * LINE_WARPS - 1) / (4 * LINE_WARPS), (T + LINE_ANGLES - 1) / LINE_ANGLES, SG);
     for (int k = 0; k < nb; ++k) {
-        if (mode != 0) {
-            auto kern = g.exact ? (mode == 2 ? k_radon_lines_shared<true, true> : k_radon_lines_shared<true, false>)
-                                : (mode == 2 ? k_radon_lines_shared<false, true> : k_radon_lines_shared<false, false>);
-            kern<<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, g.lines_nup, N, T, g.mid, k, H, nb);
-        } else if (g.exact) {
+        if (g.exact)
             k_radon_lines<true><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, g.lines_nup, N, T, g.mid,
                                                       k, H, nb);
-        } else {
+        else
             k_radon_lines<false><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, g.lines_nup, N, T,
                                                        g.mid, k, H, nb);
-        }
     }
     const size_t no = (size_t)G * nsino;
     k_lines_finish<<<grid_for(no), 256, 0, st>>>(reinterpret_cast<const float4*>(A), reinterpret_cast<float4*>(sino),
