@@ -31,6 +31,7 @@ ACU_OPT_BP_GROUPS = 10
 ACU_OPT_RADON_REFRESH = 11
 ACU_OPT_BP_PARAM_TABLE = 12
 ACU_OPT_MAX_BATCH = 13
+ACU_OPT_BP_STAGED = 14
 
 _ERRNAMES = {ACU_ERR_INVALID: "invalid argument", ACU_ERR_CUDA: "CUDA error", ACU_ERR_NOMEM: "out of memory",
              ACU_ERR_TIMEOUT: "device wait timed out", ACU_ERR_UNSUPPORTED: "unsupported"}

@@ -439,7 +439,7 @@ int tv_iterate_v(acu_ctx* c, int nouter)
         char key[400];
         snprintf(key, sizeof key, "%d/%d/%d/%d/%d/%.17g/%.17g/%d/%d/%d/%d/%d/%p/%p/%p/%p/%p/%p", (int)sizeof(Real), V,
                  s.G, s.ninner, s.ncg, s.lambda, s.mu, c->opt_filter, c->opt_projector, c->opt_positions,
-                 c->opt_residual, c->g32.d.bp_groups * 10 + c->g32.d.bp_param, s.uk.p, s.part.p, c->pairP.p,
+                 c->opt_residual, c->g32.d.bp_tma * 100 + c->g32.d.bp_groups * 10 + c->g32.d.bp_param, s.uk.p, s.part.p, c->pairP.p,
                  c->pairPT.p, c->lineL.p, c->lineA.p);
         char key2[440];
         snprintf(key2, sizeof key2, "%s/%d", key, c->opt_refresh);
@@ -880,6 +880,10 @@ int acu_set_option(acu_ctx* c, int option, int value)
         if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_BP_PARAM_TABLE must be 0 or 1");
         c->g32.d.bp_param = value;
         return ACU_OK;
+    case 14:
+        if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_BP_STAGED must be 0 or 1");
+        c->g32.d.bp_tma = value;
+        return ACU_OK;
 
     }
     return set_err(c, ACU_ERR_INVALID, "unknown option %d", option);
@@ -902,6 +906,7 @@ int acu_get_option(const acu_ctx* c, int option, int* value)
     case 13: *value = c->opt_max_batch; return ACU_OK;
     case 10: *value = c->g32.d.bp_groups; return ACU_OK;
     case 12: *value = c->g32.d.bp_param; return ACU_OK;
+    case 14: *value = c->g32.d.bp_tma; return ACU_OK;
     }
     return set_err(nullptr, ACU_ERR_INVALID, "unknown option %d", option);
 }

@@ -40,6 +40,7 @@ struct DevGeom {
     const float4* h_sc_bp = nullptr;    // host copy of sc_bp as (sin, cos, 0, 0), single precision
     int bp_param = 1;                   // backprojection: angle table in the launch parameters when T <= BP_TMAX
     int bp_groups = 0;   // slice groups per backprojection thread: 0 auto (1 with the parameter table, else 2), 1, 2 or 4
+    int bp_tma = 0;      // 1: exact backprojection from sinogram bins staged in shared memory by bulk copies
 };
 
 // ---- radon operators (kernels_radon.cu); arrays in lane layout ------------

@@ -196,6 +196,169 @@ __global__ void __launch_bounds__(256) k_backproject_exact_ct(const float* __res
     bp_exact_body<V, GPT>(q, cmask, TabParam{&tab}, img, N, T, mid);
 }
 
+// ---- backprojection with the sinogram bins staged in shared memory by the
+// bulk-copy (TMA) engine.  A block is a tile of 32 x 8 pixels (one pixel and
+// one 4-slice group per thread, exact positions, angle table in the launch
+// parameters).  For every angle, the bins the tile's pixels interpolate lie
+// between the cells of its four corners (the position is affine in the
+// pixel): that range plus one bin each side, at most 32|s| + 8|c| + 4 <= 37
+// bins of 16 bytes, is one contiguous piece of the filtered sinogram row.
+// The lanes of warp 0 copy the pieces of BPT_A angles per stage (one angle
+// each) with cp.async.bulk into one of two shared buffers, completing an
+// mbarrier with the byte count; all threads wait on it (bounded), interpolate
+// from shared memory and synchronise, and the next stage's copies overlap the
+// current stage's arithmetic.  Positions, taps, weights and summation order are those
+// of k_backproject_exact_ct: identical images.  A wait that gives up writes NaN
+// into the block's pixels (the results can never pass for valid), after
+// waiting, again bounded, for the block's copies in flight.
+constexpr int BPT_A = 24;      // angles per stage
+constexpr int BPT_BINS = 40;   // staged bins per angle (>= 37)
+
+__device__ __forceinline__ unsigned smem_u32(const void* p)
+{
+    return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned bar, unsigned parity)
+{
+    unsigned ok;
+    asm volatile("{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(ok)
+                 : "r"(bar), "r"(parity)
+                 : "memory");
+    return ok != 0;
+}
+// bounded wait: false if the phase did not complete within `limit` polls
+__device__ __forceinline__ bool mbar_wait(unsigned bar, unsigned parity, int limit)
+{
+    for (int i = 0; i < limit; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+struct BptStage {
+    float4 bins[BPT_A][BPT_BINS];
+    int lo[BPT_A];    // 1-based first staged bin of each angle
+    int cnt[BPT_A];   // staged bins of each angle
+};
+
+__global__ void __launch_bounds__(256) k_backproject_tma(const float* __restrict__ q, const float* __restrict__ cmask,
+                                                         const __grid_constant__ BpTable tab,
+                                                         float* __restrict__ img, int N, int T, float mid)
+{
+    constexpr int V = 4;
+    __shared__ __align__(128) BptStage st[2];
+    __shared__ __align__(8) unsigned long long bar[2];
+    const int tid = threadIdx.y * 32 + threadIdx.x;
+    const int jx = blockIdx.x * 32 + threadIdx.x + 1;
+    const int jy = blockIdx.y * 8 + threadIdx.y + 1;
+    const int g = blockIdx.z;
+    // tile corners (clipped to the grid)
+    const float cx0 = (float)(blockIdx.x * 32 + 1) - mid, cx1 = (float)min(blockIdx.x * 32 + 32, N) - mid;
+    const float cy0 = (float)(blockIdx.y * 8 + 1) - mid, cy1 = (float)min(blockIdx.y * 8 + 8, N) - mid;
+    const float* qg = q + (size_t)g * T * N * V;
+    const int nstage = (T + BPT_A - 1) / BPT_A;
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[0])) : "memory");
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&bar[1])) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    // warp 0: copies of stage s into buffer s & 1, lane a for angle a
+    auto issue = [&](int s) {
+        BptStage& b = st[s & 1];
+        const int lane = threadIdx.x;
+        const int t0 = s * BPT_A, na = min(BPT_A, T - t0);
+        int lo = 1, cnt = 0;
+        if (lane < na) {
+            const float4 x = tab.v[t0 + lane];
+            float c, f, cmin = 1e30f, cmax = -1e30f;
+            exact_coord(x.x, x.y, x.z, x.w, cx0, cy0, mid, c, f); cmin = fminf(cmin, c); cmax = fmaxf(cmax, c);
+            exact_coord(x.x, x.y, x.z, x.w, cx1, cy0, mid, c, f); cmin = fminf(cmin, c); cmax = fmaxf(cmax, c);
+            exact_coord(x.x, x.y, x.z, x.w, cx0, cy1, mid, c, f); cmin = fminf(cmin, c); cmax = fmaxf(cmax, c);
+            exact_coord(x.x, x.y, x.z, x.w, cx1, cy1, mid, c, f); cmin = fminf(cmin, c); cmax = fmaxf(cmax, c);
+            lo = max(1, (int)cmin - 1);
+            const int hi = min(N, (int)cmax + 2);
+            cnt = max(0, min(hi - lo + 1, BPT_BINS));
+            b.lo[lane] = lo;
+            b.cnt[lane] = cnt;
+        }
+        const unsigned bytes = __reduce_add_sync(0xffffffffu, (unsigned)cnt * 16u);
+        const unsigned bb = smem_u32(&bar[s & 1]);
+        if (lane == 0)
+            asm volatile("{\n\t.reg .b64 st;\n\tmbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(bb),
+                         "r"(bytes)
+                         : "memory");
+        __syncwarp();
+        if (cnt > 0) {
+            const float* src = qg + ((size_t)(t0 + lane) * N + (lo - 1)) * V;
+            asm volatile(
+                "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                    smem_u32(&b.bins[lane][0])),
+                "l"(src), "r"((unsigned)cnt * 16u), "r"(bb)
+                : "memory");
+        }
+    };
+    if (threadIdx.y == 0) issue(0);
+    const bool inside = jx <= N && jy <= N;
+    const size_t pix = inside ? (size_t)(jy - 1) * N + (jx - 1) : 0;
+    const float cm = inside ? cmask[pix] : 0.f;
+    const float dx = (float)jx - mid, dy = (float)jy - mid;
+    float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool ok = true;
+    int s = 0;
+    for (; s < nstage; ++s) {
+        if (threadIdx.y == 0 && s + 1 < nstage) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue(s + 1);
+        }
+        // every thread polls; the block leaves together if any gave up
+        const bool arrived = mbar_wait(smem_u32(&bar[s & 1]), (unsigned)((s >> 1) & 1), 1 << 22);
+        if (!__syncthreads_and(arrived)) {
+            ok = false;
+            break;
+        }
+        const BptStage& b = st[s & 1];
+        const int t0 = s * BPT_A, na = min(BPT_A, T - t0);
+        if (cm != 0.f) {
+            for (int a = 0; a < na; ++a) {
+                const float4 x = tab.v[t0 + a];
+                float cell, wh;
+                exact_coord(x.x, x.y, x.z, x.w, dx, dy, mid, cell, wh);
+                const int y1 = (int)cell;
+                if (y1 > 1 && y1 < N) {
+                    const float wl = 1.f - wh;
+                    const int k = y1 - b.lo[a];
+                    float4 A, B;
+                    if (k >= 0 && k + 1 < b.cnt[a]) {
+                        A = b.bins[a][k];
+                        B = b.bins[a][k + 1];
+                    } else {   // outside the staged range (never expected): read the sinogram itself
+                        const float* row = qg + ((size_t)(t0 + a) * N + (y1 - 1)) * V;
+                        A = __ldg(reinterpret_cast<const float4*>(row));
+                        B = __ldg(reinterpret_cast<const float4*>(row) + 1);
+                    }
+                    acc.x = fmaf(B.x, wh, fmaf(A.x, wl, acc.x));
+                    acc.y = fmaf(B.y, wh, fmaf(A.y, wl, acc.y));
+                    acc.z = fmaf(B.z, wh, fmaf(A.z, wl, acc.z));
+                    acc.w = fmaf(B.w, wh, fmaf(A.w, wl, acc.w));
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!ok) {
+        // a wait gave up: let the copies already issued land before the block
+        // exits (bounded), then mark the block's pixels
+        for (int r = s; r < min(s + 2, nstage); ++r) mbar_wait(smem_u32(&bar[r & 1]), (unsigned)((r >> 1) & 1), 1 << 20);
+        acc = make_float4(__int_as_float(0x7fc00000), __int_as_float(0x7fc00000), __int_as_float(0x7fc00000),
+                          __int_as_float(0x7fc00000));
+    }
+    if (inside)
+        *reinterpret_cast<float4*>(img + ((size_t)g * N * N + pix) * V) =
+            ok ? make_float4(cm * acc.x, cm * acc.y, cm * acc.z, cm * acc.w) : acc;
+}
+
 // Slice groups per thread: the angle's table entry and the sample position
 // are read and formed once for GPT groups (a warp-uniform table load still
 // costs the data pipe 32 x its width); each group's sum is unchanged.
@@ -203,6 +366,14 @@ template <typename Real, int V, int GPT>
 static void backproject_go(const DevGeom<Real>& g, int G, const Real* q, Real* img, cudaStream_t st)
 {
     dim3 blk(32, 8), grd((g.N + 31) / 32, (g.N + 7) / 8, G / GPT);
+    if constexpr (sizeof(Real) == 4 && V == 4 && GPT == 1) {
+        if (g.exact && g.bp_tma && g.bp_param && g.h_xsc_bp && g.T <= BP_TMAX) {
+            static thread_local BpTable tab;   // copied into the launch's parameters
+            std::memcpy(tab.v, g.h_xsc_bp, sizeof(float4) * g.T);
+            k_backproject_tma<<<grd, blk, 0, st>>>(q, g.cmask, tab, img, g.N, g.T, g.mid);
+            return;
+        }
+    }
     if constexpr (sizeof(Real) == 4) {
         if (g.exact) {
             if (g.bp_param && g.h_xsc_bp && g.T <= BP_TMAX) {

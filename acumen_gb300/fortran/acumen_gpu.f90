@@ -19,7 +19,7 @@ module acumen_gpu
   integer(c_int), parameter :: ACU_OPT_VERBOSE = 4, ACU_OPT_PRINT_EVERY = 5, ACU_OPT_SLICE_BASE = 6
   integer(c_int), parameter :: ACU_OPT_PROJECTOR = 7, ACU_OPT_POSITIONS = 8, ACU_OPT_RESIDUAL = 9
   integer(c_int), parameter :: ACU_OPT_BP_GROUPS = 10, ACU_OPT_RADON_REFRESH = 11
-  integer(c_int), parameter :: ACU_OPT_BP_PARAM_TABLE = 12, ACU_OPT_MAX_BATCH = 13
+  integer(c_int), parameter :: ACU_OPT_BP_PARAM_TABLE = 12, ACU_OPT_MAX_BATCH = 13, ACU_OPT_BP_STAGED = 14
 
   interface
     integer(c_int) function acu_ctx_create(ctx, nimage, ntheta, theta_deg, wpu) bind(C, name="acu_ctx_create")

@@ -77,7 +77,8 @@ def parse():
     ap.add_argument("--slices", type=int, default=S_BATCH)
     ap.add_argument("--size", type=int, default=N_GRID)
     ap.add_argument("--angles", type=int, default=T_ANG)
-    ap.add_argument("--op", default=None, choices=[None, "radon", "iradon", "backproject", "filter", "tvstep", "accuracy"],
+    ap.add_argument("--op", default=None,
+                    choices=[None, "radon", "iradon", "backproject", "filter", "tvstep", "accuracy", "prep"],
                     help="time one operator on the workload's batch (used for ncu captures); 'accuracy' prints the "
                          "full FP64 comparison of both position modes")
     ap.add_argument("--reps", type=int, default=3)
@@ -405,7 +406,7 @@ def pipeline(nproj=1200, ndet=2048, nrows=256, seed=3):
     return out
 
 
-def pipeline_device(nproj=1200, ndet=2048, nrows=256, seed=3, acc_outer=3):
+def pipeline_device(nproj=1200, ndet=2048, nrows=256, seed=3, acc_outer=3, tv=True):
     """Config 3 end to end in HBM: 1200 uint16 projections of 2048 x 256 with
     10 flat and 10 dark frames and a random rotation-axis offset in [-8, 8] px
     -> frame averages -> normalisation (mode 1) -> 0/180-degree picks ->
@@ -468,6 +469,9 @@ def pipeline_device(nproj=1200, ndet=2048, nrows=256, seed=3, acc_outer=3):
     res["axis_error_px"] = add_axis - ((nx + 1) // 2 + offset)
     del raw
     torch.cuda.empty_cache()
+    if not tv:
+        pp.close()
+        return res
     # batched TV on the pipeline's sinograms: f[slice][angle][bin]
     t = Tomography(nx, th, WPU)
     t_warm = cuda_time(lambda: t.tv_begin(sino, NINNER, NCG, LAM, MU), 1)
@@ -673,6 +677,10 @@ def run_op(args, t, f, S):
     N = args.size
     if args.op == "accuracy":
         print(json.dumps(accuracy(full=True)), flush=True)
+        return
+    if args.op == "prep":
+        # the preprocessing chain on --angles projections of 2048 x 256 (uint16, in HBM)
+        print(json.dumps(pipeline_device(nproj=args.angles, tv=False)), flush=True)
         return
     if args.op == "radon":
         img = torch.rand(S, N, N, device="cuda")

@@ -93,6 +93,10 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
                                  the device at a time (0, default: as many as fit in the free device
                                  memory); larger calls are solved in consecutive chunks of slices, each
                                  slice as in one batch */
+#define ACU_OPT_BP_STAGED 14  /* exact single-precision backprojection with the angle table in the launch
+                                 parameters: 1 stages each angle's sinogram bins of a 32x8 pixel tile in
+                                 shared memory with bulk copies (cp.async.bulk, double-buffered, mbarrier
+                                 waits bounded), 0 reads them through L1 (default); identical results */
 int acu_set_option(acu_ctx *ctx, int option, int value);
 int acu_get_option(const acu_ctx *ctx, int option, int *value);
 

@@ -293,3 +293,21 @@ def test_backprojection_table_in_parameters(built_lib):
             t.set_option(12, 0)
             assert torch.equal(a, t.backproject(q))
         t.close()
+
+
+@pytest.mark.parametrize("N, T, S", [(257, 90, 16), (1025, 300, 8), (64, 37, 4), (3, 7, 4), (129, 1920, 4)])
+def test_backprojection_staged_identical(N, T, S):
+    """ACU_OPT_BP_STAGED: the sinogram bins each 32x8 tile needs, staged in
+    shared memory by bulk copies, give the images of the L1 path bit for bit
+    (exact positions), including tiles cut by the grid's edge and angle counts
+    that leave the last stage partly filled."""
+    t = Tomography(N, syn.angles(T), 10)
+    q = torch.randn(S, T, N, device="cuda")
+    t.set_option(14, 0)
+    ref = t.backproject(q)
+    t.set_option(14, 1)
+    got = t.backproject(q)
+    assert torch.isfinite(got).all()
+    assert torch.equal(got, ref), (got - ref).abs().max().item()
+    with pytest.raises(Exception):
+        t.set_option(14, 2)
