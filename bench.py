@@ -274,7 +274,7 @@ def l1_level(achieved_gbps, clocks, probe=None, **extra):
     return out
 
 
-GOLDEN_TV = os.path.join(ROOT, "tests", "golden", "tv_1449sq_900ang.npz")
+GOLDEN_TV = {k: os.path.join(ROOT, "tests", "golden", f"tv_1449sq_900ang_{k}.npz") for k in ("input", "fp64", "fp32")}
 
 
 def tv_golden():
@@ -286,13 +286,14 @@ def tv_golden():
     import numpy as np
     import torch
     from acumen_gb300.tomography import Tomography
-    if not os.path.exists(GOLDEN_TV):
-        return {"missing": GOLDEN_TV}
-    z = np.load(GOLDEN_TV)
+    missing = [p for p in GOLDEN_TV.values() if not os.path.exists(p)]
+    if missing:
+        return {"missing": missing}
+    z = np.load(GOLDEN_TV["input"])
     N, T = int(z["params"][0]), int(z["params"][1])
     I0 = float(z["params"][2])
     f = torch.from_numpy((-np.log(z["counts"].astype(np.float64) / max(I0, 1.0))).astype(np.float32))[None].cuda()
-    ref = {"fp64": torch.from_numpy(z["tv_f64"]).cuda(), "fp32": torch.from_numpy(z["tv_f32"]).cuda()}
+    ref = {k: torch.from_numpy(np.load(GOLDEN_TV[k])["tv"]).cuda() for k in ("fp64", "fp32")}
     t = Tomography(N, z["theta"], WPU)
     mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0]
     rel = lambda a, b, m=None: float(torch.linalg.norm((a.double() - b.double())[..., m] if m is not None else

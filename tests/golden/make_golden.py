@@ -4,10 +4,10 @@ configuration: a 1449^2 grid (1448 detector bins made odd), 900 angles over
 support is the 1024-pixel disc, lambda = 0.05, mu = 1.0, wpu = 100,
 50 Bregman outer x 10 CG iterations (tomography/tv_hpc.F90:162-363).
 
-The fixture holds the counts (uint16) and the CPU oracle's TV results in the
-reference's single precision (source operation order, single-precision
-reductions: the reference's own CPU arithmetic) and in double precision
-(stored rounded to float32).  The normalised sinogram the solvers see is
+The fixture is three files: the counts (uint16) with the angles and
+parameters, and the CPU oracle's TV result in double precision (stored
+rounded to float32) and in the reference's single precision (source operation
+order, single-precision reductions: the reference's own CPU arithmetic).  The normalised sinogram the solvers see is
 p = -log(counts / I0), evaluated in double and rounded to float32, so that it
 is the same on every machine.
 
@@ -29,7 +29,8 @@ sys.path.insert(0, ROOT)
 
 N, T, I0, SEED = 1449, 900, 5e3, 2
 LAM, MU, WPU, NINNER, NOUTER, NCG = 0.05, 1.0, 100, 1, 50, 10
-OUT = os.path.join(HERE, "tv_1449sq_900ang.npz")
+INPUT = os.path.join(HERE, "tv_1449sq_900ang_input.npz")
+RESULT = {64: os.path.join(HERE, "tv_1449sq_900ang_fp64.npz"), 32: os.path.join(HERE, "tv_1449sq_900ang_fp32.npz")}
 
 
 def angles():
@@ -52,21 +53,22 @@ def normalised(c):
     return (-np.log(c.astype(np.float64) / max(I0, 1.0))).astype(np.float32)
 
 
-def main():
+def main(precisions=(64, 32)):
+    """Writes the input file, then one result file per precision as each
+    solve finishes (FP64 first)."""
     from oracle import oracle as O
     c = counts()
     f = normalised(c)
     th = angles()
-    res = {}
-    for prec, red in ((64, 1), (32, 0)):
+    np.savez_compressed(INPUT, counts=c, theta=th,
+                        params=np.array([N, T, I0, LAM, MU, WPU, NINNER, NOUTER, NCG], np.float64))
+    for prec in precisions:
+        red = 1 if prec == 64 else 0
         t0 = time.time()
         tv, _ = O.tvopt(f.astype(np.float64 if prec == 64 else np.float32), th, WPU, NINNER, NOUTER, NCG,
                         LAM, MU, prec=prec, red_mode=red)
-        res[prec] = tv.astype(np.float32)
-        print(f"oracle FP{prec}: {time.time() - t0:.0f} s", flush=True)
-    np.savez_compressed(OUT, counts=c, theta=th, tv_f32=res[32], tv_f64=res[64],
-                        params=np.array([N, T, I0, LAM, MU, WPU, NINNER, NOUTER, NCG], np.float64))
-    print("wrote", OUT, os.path.getsize(OUT), "bytes")
+        np.savez_compressed(RESULT[prec], tv=tv.astype(np.float32))
+        print(f"oracle FP{prec}: {time.time() - t0:.0f} s, wrote {RESULT[prec]}", flush=True)
 
 
 if __name__ == "__main__":

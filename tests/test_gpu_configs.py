@@ -32,7 +32,7 @@ from acumen_gb300.tomography import Tomography
 pytestmark = pytest.mark.gpu
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-GOLDEN_TV = os.path.join(HERE, "golden", "tv_1449sq_900ang.npz")
+GOLDEN = {k: os.path.join(HERE, "golden", f"tv_1449sq_900ang_{k}.npz") for k in ("input", "fp64", "fp32")}
 
 
 def rel(a, b, m=None):
@@ -79,12 +79,14 @@ def test_fbp_725sq_720ang(fbp_case, oracle, norm_mode):
 def tv_case(built_lib):
     sys.path.insert(0, os.path.join(HERE, "golden"))
     import make_golden as mg
-    if not os.path.exists(GOLDEN_TV):
-        pytest.skip("golden fixture not generated yet")
-    z = np.load(GOLDEN_TV)
+    missing = [p for p in GOLDEN.values() if not os.path.exists(p)]
+    if missing:
+        pytest.skip(f"golden fixture not generated: {missing}")
+    z = np.load(GOLDEN["input"])
     assert int(z["params"][0]) == mg.N and int(z["params"][1]) == mg.T
     f = mg.normalised(z["counts"])
-    return dict(mg=mg, f=f, th=z["theta"], tv32=z["tv_f32"], tv64=z["tv_f64"])
+    ref = {k: np.load(GOLDEN[k])["tv"] for k in ("fp64", "fp32")}
+    return dict(mg=mg, f=f, th=z["theta"], tv32=ref["fp32"], tv64=ref["fp64"])
 
 
 def _solve(case, positions, plain=False):
