@@ -598,11 +598,11 @@ def gradient_config5(S=32, N=N_GRID, T=1500, seed=11):
            "device_bytes_held_by_call": int(free0 - free1),
            "inputs_bytes": int(4 * (2 * S * N * N + S * T * N + S * T)),
            "grad_u_f32_rel_l2_vs_f64": rel(gu[:1], gu64), "grad_off_f32_rel_l2_vs_f64": rel(go[:1], go64),
-           "loss_f32_rel_vs_f64": abs(float(loss[0]) - float(l64)) / abs(float(l64))}
+           "loss_f32_rel_vs_f64": abs(float(np.ravel(loss)[0]) - float(np.ravel(l64)[0])) / abs(float(np.ravel(l64)[0]))}
     h = 1e-3
 
     def f64loss(uu, oo):
-        return float(t.tv_loss_grad(uu, oo, y0, LAMG, EPS, want_grad=False)[0])
+        return float(np.ravel(t.tv_loss_grad(uu, oo, y0, LAMG, EPS, want_grad=False)[0])[0])
 
     fd_u, fd_o = [], []
     for _ in range(3):
