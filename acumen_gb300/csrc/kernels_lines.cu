@@ -24,6 +24,7 @@
 // (x1+1,y1+1)), so the sums are bit-identical to variants 1 to 5.  Two bands
 // of H + 1 rows of one super-group are a launch's working set.
 #include <algorithm>
+#include <atomic>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -423,9 +424,19 @@ void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float*
     dim3 blk(32, LINE_WARPS * LINE_NA);
     dim3 grd((N + 4 * LINE_WARPS - 1) / (4 * LINE_WARPS), (T + LINE_ANGLES - 1) / LINE_ANGLES, SG);
     if (staged) {
+        // the two buffers (108 KB) need the opt-in above the default 48 KB;
+        // the attribute counts only dynamic shared memory, and together with
+        // the kernel's static barriers it must stay within the 227 KB limit
         const size_t smem = sizeof(float) * 2 * ST_LINES * LINE_W;
-        max_dynamic_smem<k_radon_lines_staged<true>>();
-        max_dynamic_smem<k_radon_lines_staged<false>>();
+        static std::atomic<unsigned long long> set{0};   // per device, once
+        int dev = 0;
+        cudaGetDevice(&dev);
+        const unsigned long long bit = 1ull << (dev & 63);
+        if (!(set.load(std::memory_order_acquire) & bit)) {
+            cudaFuncSetAttribute(k_radon_lines_staged<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            cudaFuncSetAttribute(k_radon_lines_staged<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+            set.fetch_or(bit, std::memory_order_release);
+        }
         dim3 sgrd((N + 4 * LINE_WARPS - 1) / (4 * LINE_WARPS), (T + LINE_NA - 1) / LINE_NA, SG);
         for (int k = 0; k < nb; ++k) {
             if (g.exact)
