@@ -149,6 +149,73 @@ __global__ void __launch_bounds__(32 * LINE_WARPS * LINE_NA, 5) k_radon_lines(
     }
 }
 
+// ---- variants 9 to 11: the band walk with NA angles per block walked in
+// lockstep.  A block holds 16 rays of each of NA consecutive angles (of
+// `order`, so neighbouring angles), one quarter-warp per ray as in variant 6.
+// Its warps walk the union of their rays' steps in the band in chunks of CH
+// steps and meet at a block barrier after each chunk, so at any time the
+// block's samples lie in one short stretch of its ray bundles: the pixel lines
+// that stretch needs are fetched into L1 once and read by all NA angles.  The
+// bundles of neighbouring angles overlap (0.15 degrees apart they diverge by
+// ~2.6 px per 1000 px from the centre), so the L2 traffic per sample falls
+// roughly as (17 + (NA-1) 2.6 r/1000) / (16 NA).  Samples, taps and order are
+// those of variant 6: identical sums.
+template <bool EX, int NA, int CH>
+__global__ void __launch_bounds__(32 * LINE_WARPS * NA, (NA == 2 ? 5 : NA == 4 ? 2 : 1)) k_radon_lines_lock(
+    const float* __restrict__ L, float* __restrict__ A, const float* __restrict__ sc, const float4* __restrict__ xsc,
+    const int* __restrict__ order, int nup, int N, int T, float mid, int step, int H, int nb)
+{
+    __shared__ int rng[2];
+    const int lane = threadIdx.x & 31, q = lane >> 3, h = lane & 7;
+    const int warp = threadIdx.y;
+    const int jy = blockIdx.x * (4 * LINE_WARPS) + (warp % LINE_WARPS) * 4 + q + 1;
+    const int slot = warp / LINE_WARPS;
+    const size_t sg = blockIdx.z;
+    const float* p0 = L + sg * N * N * LINE_W + h * 4;
+    const int ti = blockIdx.y * NA + slot;               // warp-uniform
+    const bool ok = ti < T && jy <= N;
+    const int t = order[ti < T ? ti : T - 1];
+    const int jyc = jy <= N ? jy : N;
+    const float s = sc[2 * t], c = sc[2 * t + 1];
+    const int b = ti < nup ? step : nb - 1 - step;
+    const int ylo = 2 + b * H, yhi = min(N - 1, 1 + (b + 1) * H);
+    int lo = 1, hi = 0;
+    if (ok && ylo <= yhi) {
+        valid_steps(s, c, (float)jyc - mid, mid, N, lo, hi);
+        band_steps(s, c, (float)jyc - mid, mid, N, ylo, yhi, lo, hi);
+    }
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        rng[0] = 0x7fffffff;
+        rng[1] = -0x7fffffff;
+    }
+    __syncthreads();
+    if (lo <= hi) {
+        atomicMin(&rng[0], lo);
+        atomicMax(&rng[1], hi);
+    }
+    __syncthreads();
+    const int J0 = rng[0], J1 = rng[1];
+    if (J0 > J1) return;                                 // block-uniform
+    float acc[4] = {0.f, 0.f, 0.f, 0.f};
+    float4* ap = reinterpret_cast<float4*>(A + ((sg * T + t) * N + (jyc - 1)) * LINE_W + h * 4);
+    if (lo <= hi) {
+        const float4 a = *ap;
+        acc[0] = a.x;
+        acc[1] = a.y;
+        acc[2] = a.z;
+        acc[3] = a.w;
+    }
+    const ProjRay<float, EX> ray(sc, xsc, t, jyc, mid, nullptr);
+    const bool cols = fabsf(c) > fabsf(s);
+    for (int j = J0; j <= J1; j += CH) {
+        const int a = max(lo, j), e = min(hi, j + CH - 1);
+        if (cols) line_segment<EX, true>(p0, N, a, e, ray, mid, ylo, yhi, acc);
+        else line_segment<EX, false>(p0, N, a, e, ray, mid, ylo, yhi, acc);
+        __syncthreads();
+    }
+    if (lo <= hi) *ap = make_float4(acc[0], acc[1], acc[2], acc[3]);
+}
+
 // ---- variant 8: the band walk with each block's pixel lines staged in shared
 // memory by the bulk-copy (TMA) engine.  A block is the same 16 rays x 2
 // angles as variant 6 (one angle pair per block).  It walks the union of its
@@ -410,8 +477,24 @@ int lines_band_rows(int N)
 size_t lines_image_floats(int N, int G) { return (size_t)((G + 7) / 8) * N * N * LINE_W; }
 size_t lines_sums_floats(int N, int T, int G) { return (size_t)((G + 7) / 8) * T * N * LINE_W; }
 
+template <int NA, int CH>
+static void lock_launch(const DevGeom<float>& g, int SG, const float* L, float* A, int H, int nb, cudaStream_t st)
+{
+    const int N = g.N, T = g.T;
+    dim3 blk(32, LINE_WARPS * NA);
+    dim3 grd((N + 4 * LINE_WARPS - 1) / (4 * LINE_WARPS), (T + NA - 1) / NA, SG);
+    for (int k = 0; k < nb; ++k) {
+        if (g.exact)
+            k_radon_lines_lock<true, NA, CH><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, g.lines_nup,
+                                                                  N, T, g.mid, k, H, nb);
+        else
+            k_radon_lines_lock<false, NA, CH><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order,
+                                                                   g.lines_nup, N, T, g.mid, k, H, nb);
+    }
+}
+
 void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float* L, float* A, float* sino,
-                        cudaStream_t st, bool staged)
+                        cudaStream_t st, int mode)
 {
     const int N = g.N, T = g.T, SG = (G + 7) / 8;
     if (G <= 0 || N <= 0 || T <= 0) return;
@@ -423,6 +506,10 @@ void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float*
     const int H = lines_band_rows(N), nb = std::max(1, (N - 2 + H - 1) / H);
     dim3 blk(32, LINE_WARPS * LINE_NA);
     dim3 grd((N + 4 * LINE_WARPS - 1) / (4 * LINE_WARPS), (T + LINE_ANGLES - 1) / LINE_ANGLES, SG);
+    const bool staged = mode == 1;
+    if (mode == 2) lock_launch<2, 16>(g, SG, L, A, H, nb, st);
+    if (mode == 3) lock_launch<4, 16>(g, SG, L, A, H, nb, st);
+    if (mode == 4) lock_launch<8, 16>(g, SG, L, A, H, nb, st);
     if (staged) {
         // the two buffers (108 KB) need the opt-in above the default 48 KB;
         // the attribute counts only dynamic shared memory, and together with
@@ -447,7 +534,7 @@ void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float*
                                                                       g.lines_nup, N, T, g.mid, k, H, nb);
         }
     }
-    for (int k = 0; k < (staged ? 0 : nb); ++k) {
+    for (int k = 0; k < (mode != 0 ? 0 : nb); ++k) {
         if (g.exact)
             k_radon_lines<true><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, g.lines_nup, N, T, g.mid,
                                                       k, H, nb);

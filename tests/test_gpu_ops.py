@@ -169,14 +169,14 @@ def test_projector_variants_agree(case, oracle):
     for x in (case["img"][:5].astype(np.float32), rng.standard_normal((5, case["N"], case["N"])).astype(np.float32)):
         img = torch.from_numpy(x).cuda()
         outs = []
-        for v in (0, 1, 2, 3, 4, 5, 6, 8):
+        for v in (0, 1, 2, 3, 4, 5, 6, 8, 9, 10, 11):
             t.set_option(7, v)
             outs.append(t.radon(img))
         # reusing the previous sample's taps, skipping steps that cannot meet
         # a valid cell, pairing the FMAs, walking the rays in bands of pixel
         # lines and staging those lines in shared memory change neither values
         # nor order
-        assert all(torch.equal(outs[k], outs[1]) for k in range(3, 8))
+        assert all(torch.equal(outs[k], outs[1]) for k in range(3, 11))
         ref = oracle.radon(x, case["th"], 32)
         for o in outs:
             assert rel(o, ref) < 1e-6
@@ -253,7 +253,7 @@ def test_line_projector_bitwise(N, T, S, wpu):
         t.set_option(8, ex)
         t.set_option(7, 5)
         ref = t.radon(x)
-        for v in (6, 8):
+        for v in (6, 8, 9, 10, 11):
             t.set_option(7, v)
             got = t.radon(x)
             assert torch.equal(got, ref), (ex, v, (got - ref).abs().max().item())
