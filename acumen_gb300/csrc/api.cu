@@ -177,7 +177,7 @@ int ensure_projector_buffers(acu_ctx* c, int G)
     if (v == 0) {
         CK(c, c->pairP.ensure(sizeof(float) * 2 * nimg));
         CK(c, c->pairPT.ensure(sizeof(float) * 2 * nimg));
-    } else if (v == 6 || v >= 8) {
+    } else if (v == 6) {
         CK(c, c->lineL.ensure(sizeof(float) * lines_image_floats(c->N, G)));
         CK(c, c->lineA.ensure(sizeof(float) * lines_sums_floats(c->N, c->T, G)));
     } else {
@@ -191,9 +191,8 @@ int ensure_projector_buffers(acu_ctx* c, int G)
 void radon_quads(acu_ctx* c, const DevGeom<float>& g, int G, const float* img, float* sino)
 {
     const int v = projector_variant(c, G);
-    if (v == 6 || v >= 8)
-        launch_radon_lines(g, G, img, c->lineL.as<float>(), c->lineA.as<float>(), sino, c->stream,
-                           v == 6 ? 0 : v - 7);
+    if (v == 6)
+        launch_radon_lines(g, G, img, c->lineL.as<float>(), c->lineA.as<float>(), sino, c->stream);
     else if (v >= 1)
         launch_radon_quads(g, G, img, c->pairPT.as<float>(), sino, c->stream, v == 2, v >= 3, v >= 4, v == 5);
     else
@@ -572,7 +571,7 @@ int tv_chunk(acu_ctx* c, int S, bool host_io)
     const int proj = c->opt_projector == 7 ? 6 : c->opt_projector;
     size_t per = sizeof(Real) * (5 * T * N + 10 * N * N);
     if (sizeof(Real) == 4)
-        per += sizeof(float) * (proj == 0 ? 4 * N * N : (proj == 6 || proj >= 8) ? N * N + T * N : N * N);
+        per += sizeof(float) * (proj == 0 ? 4 * N * N : proj == 6 ? N * N + T * N : N * N);
     if (host_io) per += sizeof(float) * (T * N + 2 * N * N);
     size_t freeb = 0, totalb = 0;
     if (cudaMemGetInfo(&freeb, &totalb) != cudaSuccess) freeb = 0;
@@ -852,7 +851,7 @@ int acu_set_option(acu_ctx* c, int option, int value)
         return ACU_OK;
     case 6: c->opt_slice_base = value; return ACU_OK;
     case 7:
-        if (value < 0 || value > 11) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 to 11");
+        if (value < 0 || value > 7) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_PROJECTOR must be 0 to 7");
         c->opt_projector = value;
         return ACU_OK;
     case 8:

@@ -62,11 +62,8 @@ void launch_radon_quads(const DevGeom<float>& g, int G, const float* img, float*
 // Projector variant 6 (kernels_lines.cu): the batch regrouped into 128-byte
 // pixel lines of 32 slices, walked in bands of rows that stay in L2.  L and A
 // are work buffers of lines_image_floats and lines_sums_floats floats.
-// mode 1 (variant 8): each block's pixel lines copied into shared memory by
-// bulk copies, chunk by chunk; modes 2, 3, 4 (variants 9, 10, 11): 2, 4 or 8
-// angles per block walked in lockstep chunks of 16 steps; identical sums.
 void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float* L, float* A, float* sino,
-                        cudaStream_t st, int mode = 0);
+                        cudaStream_t st);
 size_t lines_image_floats(int N, int G);
 size_t lines_sums_floats(int N, int T, int G);
 int lines_band_rows(int N);

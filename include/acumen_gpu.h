@@ -70,9 +70,7 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
                                  to those that can meet a valid cell, 5 the same with paired FP32 FMAs
                                  (fma.rn.f32x2), 6 pixel lines of 32 slices walked in bands of rows,
                                  7 automatic (default): 6 when the batch fills its 32-slice lines to
-                                 8/9 or more, else 5; 8 variant 6 with each block's pixel lines staged
-                                 in shared memory by bulk copies (cp.async.bulk, mbarrier waits bounded);
-                                 1, 3 to 6 and 8 give identical results */
+                                 8/9 or more, else 5; 1 and 3 to 6 give identical results */
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 1 exact (default; coordinates from split
                                  FP64 angle tables, within ~1e-7 px of FP64: the mode that meets relL2
                                  1e-5 FBP / 1e-4 TV against FP64 at the benchmark sizes), 0 the

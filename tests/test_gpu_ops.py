@@ -169,14 +169,13 @@ def test_projector_variants_agree(case, oracle):
     for x in (case["img"][:5].astype(np.float32), rng.standard_normal((5, case["N"], case["N"])).astype(np.float32)):
         img = torch.from_numpy(x).cuda()
         outs = []
-        for v in (0, 1, 2, 3, 4, 5, 6, 8, 9, 10, 11):
+        for v in range(7):
             t.set_option(7, v)
             outs.append(t.radon(img))
         # reusing the previous sample's taps, skipping steps that cannot meet
-        # a valid cell, pairing the FMAs, walking the rays in bands of pixel
-        # lines and staging those lines in shared memory change neither values
-        # nor order
-        assert all(torch.equal(outs[k], outs[1]) for k in range(3, 11))
+        # a valid cell, pairing the FMAs and walking the rays in bands of
+        # pixel lines change neither values nor order
+        assert all(torch.equal(outs[v], outs[1]) for v in range(3, 7))
         ref = oracle.radon(x, case["th"], 32)
         for o in outs:
             assert rel(o, ref) < 1e-6
@@ -239,10 +238,9 @@ def test_exact_positions_projector_and_adjoint(oracle, built_lib):
 @pytest.mark.parametrize("N, T, S, wpu", [(725, 97, 37, 20), (1025, 60, 4, 30), (2049, 24, 33, 100), (64, 37, 9, 6),
                                            (3, 11, 4, 1)])
 def test_line_projector_bitwise(N, T, S, wpu):
-    """Projector variants 6 and 8 (pixel lines of 32 slices, rays walked in
-    bands of rows, several bands from N = 725 on; 8 stages each block's lines
-    in shared memory by bulk copies) give bit for bit the sums of variant 5,
-    in both position modes, on random images that reach the
+    """Projector variant 6 (pixel lines of 32 slices, rays walked in bands of
+    rows, several bands from N = 725 on) gives bit for bit the sums of
+    variant 5, in both position modes, on random images that reach the
     border, with slice counts that leave super-groups partly empty and
     angles on and near the axes."""
     th = np.concatenate([syn.angles(T - 8), [0.0, 45.0, 90.0, 135.0, 180.0, 89.9999, 90.0001, 1e-5]])
@@ -253,7 +251,7 @@ def test_line_projector_bitwise(N, T, S, wpu):
         t.set_option(8, ex)
         t.set_option(7, 5)
         ref = t.radon(x)
-        for v in (6, 8, 9, 10, 11):
+        for v in (6,):
             t.set_option(7, v)
             got = t.radon(x)
             assert torch.equal(got, ref), (ex, v, (got - ref).abs().max().item())
