@@ -67,6 +67,30 @@ __global__ void __launch_bounds__(256) k_backproject(const Real* __restrict__ q,
     }
 }
 
+// acc += a wl + b wh slice by slice, as two fused multiply-adds in that order;
+// four slices as paired FMAs (fma.rn.f32x2, each half rounded as fmaf), which
+// halves the instructions of the backprojection's inner loop.
+template <int V>
+__device__ __forceinline__ void lerp_acc(Lanes<float, V>& acc, const Lanes<float, V>& a, const Lanes<float, V>& b,
+                                         float wl, float wh)
+{
+    if constexpr (V == 4) {
+        const float2 WL = make_float2(wl, wl), WH = make_float2(wh, wh);
+        float2 lo = make_float2(acc.v[0], acc.v[1]), hi = make_float2(acc.v[2], acc.v[3]);
+        lo = fma2(make_float2(a.v[0], a.v[1]), WL, lo);
+        hi = fma2(make_float2(a.v[2], a.v[3]), WL, hi);
+        lo = fma2(make_float2(b.v[0], b.v[1]), WH, lo);
+        hi = fma2(make_float2(b.v[2], b.v[3]), WH, hi);
+        acc.v[0] = lo.x;
+        acc.v[1] = lo.y;
+        acc.v[2] = hi.x;
+        acc.v[3] = hi.y;
+    } else {
+#pragma unroll
+        for (int v = 0; v < V; ++v) acc.v[v] = fmaf(b.v[v], wh, fmaf(a.v[v], wl, acc.v[v]));
+    }
+}
+
 // k_backproject in single precision with the per-angle (sin, cos) read from
 // the launch parameters (constant-cache broadcast; T <= BP_TMAX).
 template <int V, int GPT>
@@ -103,8 +127,7 @@ __global__ void __launch_bounds__(256) k_backproject_ct(const float* __restrict_
                     const float* row = qg + ((size_t)(k * T + t) * N + (y1 - 1)) * V;
                     const Lanes<float, V> a = ld_lanes<float, V>(row);
                     const Lanes<float, V> b = ld_lanes<float, V>(row + V);
-#pragma unroll
-                    for (int v = 0; v < V; ++v) acc[k].v[v] = fmaf(b.v[v], wh, fmaf(a.v[v], wl, acc[k].v[v]));
+                    lerp_acc<V>(acc[k], a, b, wl, wh);
                 }
             }
         }
@@ -164,8 +187,7 @@ __device__ __forceinline__ void bp_exact_body(const float* __restrict__ q, const
                     const float* row = qg + ((size_t)(k * T + t) * N + (y1 - 1)) * V;
                     const Lanes<float, V> a = ld_lanes<float, V>(row);
                     const Lanes<float, V> b = ld_lanes<float, V>(row + V);
-#pragma unroll
-                    for (int v = 0; v < V; ++v) acc[k].v[v] = fmaf(b.v[v], wh, fmaf(a.v[v], wl, acc[k].v[v]));
+                    lerp_acc<V>(acc[k], a, b, wl, wh);
                 }
             }
         }
