@@ -286,14 +286,14 @@ def tv_golden():
     import numpy as np
     import torch
     from acumen_gb300.tomography import Tomography
-    missing = [p for p in GOLDEN_TV.values() if not os.path.exists(p)]
-    if missing:
-        return {"missing": missing}
+    if not os.path.exists(GOLDEN_TV["input"]) or not os.path.exists(GOLDEN_TV["fp64"]):
+        return {"missing": [p for p in GOLDEN_TV.values() if not os.path.exists(p)]}
     z = np.load(GOLDEN_TV["input"])
     N, T = int(z["params"][0]), int(z["params"][1])
     I0 = float(z["params"][2])
     f = torch.from_numpy((-np.log(z["counts"].astype(np.float64) / max(I0, 1.0))).astype(np.float32))[None].cuda()
-    ref = {k: torch.from_numpy(np.load(GOLDEN_TV[k])["tv"]).cuda() for k in ("fp64", "fp32")}
+    ref = {k: torch.from_numpy(np.load(GOLDEN_TV[k])["tv"]).cuda() for k in ("fp64", "fp32")
+           if os.path.exists(GOLDEN_TV[k])}
     t = Tomography(N, z["theta"], WPU)
     mask = (t.backproject(torch.ones(1, T, N, device="cuda")) != 0)[0]
     rel = lambda a, b, m=None: float(torch.linalg.norm((a.double() - b.double())[..., m] if m is not None else
@@ -306,11 +306,13 @@ def tv_golden():
         for path, plain in (("batched", False), ("plain", True)):
             tv, _ = t.tvopt(f, NINNER, NOUTER, NCG, LAM, MU, plain=plain)
             tv = tv[0]
-            out[f"{name}_positions_{path}"] = {
-                "rel_l2_disc_vs_fp64": rel(tv, ref["fp64"], mask), "rel_l2_full_vs_fp64": rel(tv, ref["fp64"]),
-                "rel_l2_disc_vs_fp32_oracle": rel(tv, ref["fp32"], mask),
-                "rel_l2_full_vs_fp32_oracle": rel(tv, ref["fp32"])}
-    out["fp32_oracle_rel_l2_disc_vs_fp64"] = rel(ref["fp32"], ref["fp64"], mask)
+            r = {"rel_l2_disc_vs_fp64": rel(tv, ref["fp64"], mask), "rel_l2_full_vs_fp64": rel(tv, ref["fp64"])}
+            if "fp32" in ref:
+                r.update({"rel_l2_disc_vs_fp32_oracle": rel(tv, ref["fp32"], mask),
+                          "rel_l2_full_vs_fp32_oracle": rel(tv, ref["fp32"])})
+            out[f"{name}_positions_{path}"] = r
+    if "fp32" in ref:
+        out["fp32_oracle_rel_l2_disc_vs_fp64"] = rel(ref["fp32"], ref["fp64"], mask)
     out["seconds"] = time.perf_counter() - t0
     t.close()
     return out

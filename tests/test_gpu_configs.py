@@ -79,13 +79,10 @@ def test_fbp_725sq_720ang(fbp_case, oracle, norm_mode):
 def tv_case(built_lib):
     sys.path.insert(0, os.path.join(HERE, "golden"))
     import make_golden as mg
-    missing = [p for p in GOLDEN.values() if not os.path.exists(p)]
-    if missing:
-        pytest.skip(f"golden fixture not generated: {missing}")
     z = np.load(GOLDEN["input"])
     assert int(z["params"][0]) == mg.N and int(z["params"][1]) == mg.T
     f = mg.normalised(z["counts"])
-    ref = {k: np.load(GOLDEN[k])["tv"] for k in ("fp64", "fp32")}
+    ref = {k: np.load(GOLDEN[k])["tv"] if os.path.exists(GOLDEN[k]) else None for k in ("fp64", "fp32")}
     return dict(mg=mg, f=f, th=z["theta"], tv32=ref["fp32"], tv64=ref["fp64"])
 
 
@@ -100,6 +97,8 @@ def _solve(case, positions, plain=False):
 
 
 def test_tv_1449sq_900ang_exact_positions_vs_fp64_golden(tv_case, oracle):
+    if tv_case["tv64"] is None:
+        pytest.skip("golden FP64 result not generated")
     mg = tv_case["mg"]
     mask = oracle.cmask(mg.N, mg.T, mg.WPU, 64) > 0
     tv = _solve(tv_case, 1)
@@ -108,6 +107,8 @@ def test_tv_1449sq_900ang_exact_positions_vs_fp64_golden(tv_case, oracle):
 
 
 def test_tv_1449sq_900ang_reference_positions_vs_fp32_golden(tv_case, oracle):
+    if tv_case["tv32"] is None:
+        pytest.skip("golden FP32 result not generated")
     mg = tv_case["mg"]
     mask = oracle.cmask(mg.N, mg.T, mg.WPU, 64) > 0
     for plain in (False, True):
