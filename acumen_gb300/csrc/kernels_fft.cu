@@ -51,16 +51,19 @@ __device__ __forceinline__ C csub(C a, C b)
 
 // Forward DFT of length L (power of two >= 16) held in d0; returns the buffer
 // holding the natural-order result (d0 or d1).
+// Ns and L are powers of two: indices are formed with shifts and masks.
 template <typename C>
 __device__ C* fft_stockham(C* d0, C* d1, const C* __restrict__ tw, int L)
 {
-    for (int Ns = 1; Ns < L;) {
-        const int R = ((L / Ns) % 4 == 0) ? 4 : 2;
-        const int stride = L / (Ns * R);
-        const int nb = L / R;
+    const int lgL = 31 - __clz(L);
+    for (int Ns = 1, lgNs = 0; Ns < L;) {
+        const int R = ((lgL - lgNs) >= 2) ? 4 : 2;
+        const int lgR = R == 4 ? 2 : 1;
+        const int stride = L >> (lgNs + lgR);
+        const int nb = L >> lgR;
         for (int j = threadIdx.x; j < nb; j += blockDim.x) {
-            const int k = j % Ns;
-            const int idxD = (j / Ns) * Ns * R + k;
+            const int k = j & (Ns - 1);
+            const int idxD = ((j >> lgNs) << (lgNs + lgR)) + k;
             if (R == 4) {
                 C v0 = d0[j];
                 C v1 = cmul(d0[j + nb], tw[k * stride]);
@@ -85,7 +88,8 @@ __device__ C* fft_stockham(C* d0, C* d1, const C* __restrict__ tw, int L)
         C* t = d0;
         d0 = d1;
         d1 = t;
-        Ns *= R;
+        Ns <<= lgR;
+        lgNs += lgR;
     }
     return d0;
 }
@@ -118,10 +122,16 @@ __global__ void __launch_bounds__(256) k_filter_fft(const Real* __restrict__ sin
         stride = 1;
         has_b = (t0 + 1) < T;
     }
+    // 4-slice lanes: the two columns of a half-lane sit side by side (8 or 16
+    // bytes, aligned), so they move as one vector
     for (int n = threadIdx.x; n < L; n += blockDim.x) {
         C z;
-        z.x = n < N ? sino[offa + (size_t)n * stride] : Real(0);
-        z.y = (n < N && has_b) ? sino[offb + (size_t)n * stride] : Real(0);
+        if (V == 4) {
+            z = n < N ? __ldg(reinterpret_cast<const C*>(sino + offa + (size_t)n * 4)) : C{Real(0), Real(0)};
+        } else {
+            z.x = n < N ? sino[offa + (size_t)n * stride] : Real(0);
+            z.y = (n < N && has_b) ? sino[offb + (size_t)n * stride] : Real(0);
+        }
         d0[n] = z;
     }
     __syncthreads();
@@ -140,8 +150,12 @@ __global__ void __launch_bounds__(256) k_filter_fft(const Real* __restrict__ sin
     C* y = fft_stockham<C>(res, other, tw, L);
     for (int n = threadIdx.x; n < N; n += blockDim.x) {
         const C v = y[n];
-        out[offa + (size_t)n * stride] = v.x;
-        if (has_b) out[offb + (size_t)n * stride] = -v.y;
+        if (V == 4) {
+            *reinterpret_cast<C*>(out + offa + (size_t)n * 4) = C{v.x, -v.y};
+        } else {
+            out[offa + (size_t)n * stride] = v.x;
+            if (has_b) out[offb + (size_t)n * stride] = -v.y;
+        }
     }
 }
 
