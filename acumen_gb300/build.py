@@ -62,7 +62,7 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     return OUT
 
 
-DRIVERS = ["fits_to_hpc", "raw_to_hpc", "projections_to_sinogram_hpc", "fbp_hpc", "tv_hpc", "tv_hpc_slice"]
+DRIVERS = ["fits_to_hpc", "raw_to_hpc", "projections_to_sinogram_hpc", "fbp_hpc", "tv_hpc", "tv_hpc_slice", "to_tiff"]
 BIN = os.path.join(HERE, "bin")
 
 
