@@ -3,11 +3,16 @@
 // slice of the reconstructions, or every projection and sinogram, written as
 // one TIFF file.
 //
-//   to_tiff [fbp|sino]        ($ROOT_CT_DIR, $EXP_CT_NAME as the drivers)
+//   to_tiff [fbp|sub|sino]    ($ROOT_CT_DIR, $EXP_CT_NAME as the drivers)
 //
 // fbp  (convert_to_tiff.m:31-63): slice j of fbp{k}.dat and fbp_tv{k}.dat ->
 //      $ROOT_CT_DIR/$EXP_CT_NAME/fbp_images/fbp{j}.tiff and
 //      fbp_tv_images/fbp_tv{j}.tiff, (nimage+add)^2 pixels each;
+// sub  (convert_sub_to_tiff.m:31-64): the same for the sub-sampled results
+//      fbp_sub{k}.dat and fbp_sub_tv{k}.dat -> fbp_sub_images/,
+//      fbp_sub_tv_images/; the image side is the one tv_hpc writes with
+//      Sub_Sample_Radial = nsub, floor((nimage+add-1)/nsub)+1 (the MATLAB
+//      script reads (nimage+add)^2, right only for nsub = 1);
 // sino (projections_sino_tiff.m:34-63): projection j of projections{k}.dat ->
 //      projections_images/projections{j}.tiff (nimage^2) and slice j of
 //      sinograms{k}.dat -> sinogram_images/sinogram{j}.tiff
@@ -26,8 +31,11 @@
 // counts agree, so here both use n_files_rec, as fbp_hpc and tv_hpc write.
 #include <sys/stat.h>
 
+#include <cerrno>
+#include <cmath>
 #include <cstdint>
 #include <cstdio>
+#include <cstring>
 #include <iostream>
 
 #include "hpc_io.h"
@@ -143,7 +151,7 @@ int main(int argc, char** argv)
 {
     try {
         const std::string mode = argc > 1 ? argv[1] : "fbp";
-        if (mode != "fbp" && mode != "sino") throw Fail("usage: to_tiff [fbp|sino]");
+        if (mode != "fbp" && mode != "sub" && mode != "sino") throw Fail("usage: to_tiff [fbp|sub|sino]");
         const bool as_float = env("ACUMEN_TIFF", false) == "float";
         const std::string rec = recon_dir();
         const std::string wdir = env("ROOT_CT_DIR") + "/" + env("EXP_CT_NAME") + "/";
@@ -152,8 +160,13 @@ int main(int argc, char** argv)
         const int n = fi.nimage + add;
         std::vector<float> buf;
         int written = 0;
-        if (mode == "fbp") {
-            for (const std::string base : {"fbp", "fbp_tv"}) {
+        if (mode == "fbp" || mode == "sub") {
+            const bool sub = mode == "sub";
+            const std::string ns = env("Sub_Sample_Radial", false);
+            const int nsub = sub && !ns.empty() ? std::atoi(ns.c_str()) : 1;
+            if (nsub < 1) throw Fail("Sub_Sample_Radial must be >= 1");
+            const int side = (int)std::floor((float)(n - 1) / (float)nsub) + 1;
+            for (const std::string base : {sub ? "fbp_sub" : "fbp", sub ? "fbp_sub_tv" : "fbp_tv"}) {
                 if (!exists(rec + fnum(base, 1))) {
                     std::cout << "no " << base << "1.dat: skipped\n";
                     continue;
@@ -161,9 +174,9 @@ int main(int argc, char** argv)
                 const std::string out = wdir + base + "_images/";
                 make_dir(out);
                 for (int j = 1; j <= fi.nimage; ++j) {
-                    if (!read_item(rec, base, j, fi.nimage, fi.n_files_rec, (size_t)n * n, buf))
+                    if (!read_item(rec, base, j, fi.nimage, fi.n_files_rec, (size_t)side * side, buf))
                         throw Fail("missing file for " + base + " slice " + std::to_string(j));
-                    write_tiff(out + base + std::to_string(j) + ".tiff", buf.data(), n, n, as_float);
+                    write_tiff(out + base + std::to_string(j) + ".tiff", buf.data(), side, side, as_float);
                     ++written;
                 }
             }

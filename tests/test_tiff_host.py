@@ -97,6 +97,26 @@ def test_reconstruction_images(dataset):
             np.testing.assert_array_equal(img, matlab_u8(ref[j - 1].astype(np.float32).T))
 
 
+def test_sub_sampled_images(dataset, tmp_path):
+    """Sub-sampled results (tv_hpc with Sub_Sample_Radial = 2): side
+    floor((nimage + add - 1) / 2) + 1 = 4 for nimage = 6."""
+    rec = tmp_path / "s" / "reconstruction"
+    rec.mkdir(parents=True)
+    np.array([NFILES, NIMG, NSINO, NREC], np.float32).tofile(rec / "fileinfo_projections.dat")
+    rng = np.random.default_rng(1)
+    side = (NIMG + 1 - 1) // 2 + 1
+    sub = [rng.uniform(-0.3, 1.3, (side, side)) for _ in range(NIMG)]
+    subtv = [rng.uniform(-0.3, 1.3, (side, side)) for _ in range(NIMG)]
+    write_split(rec, "fbp_sub", sub, NREC)
+    write_split(rec, "fbp_sub_tv", subtv, NREC)
+    env = dict(os.environ, ROOT_CT_DIR=str(tmp_path), EXP_CT_NAME="s", Sub_Sample_Radial="2")
+    assert f"{2 * NIMG} images" in run(env, "sub")
+    for j in range(1, NIMG + 1):
+        for base, ref in (("fbp_sub", sub), ("fbp_sub_tv", subtv)):
+            img = read_tiff(tmp_path / "s" / f"{base}_images" / f"{base}{j}.tiff")
+            np.testing.assert_array_equal(img, matlab_u8(ref[j - 1].astype(np.float32).T))
+
+
 def test_projection_and_sinogram_images_as_floats(dataset):
     env = dict(dataset["env"], ACUMEN_TIFF="float")
     run(env, "sino")
