@@ -771,6 +771,8 @@ def main():
     per_radon = radon_launches(variant, N)
     kernel_launches = (per_radon * n_radon + 2 * n_iradon + n_ew) * args.steps + per_radon * n_full
 
+    # solver state: 10 image-sized and 5 sinogram-sized FP32 arrays per slice
+    state_gb = S * (10 * N * N + 5 * T * N) * 4 / 1e9
     line = {"metric": METRIC, "value": value, "unit": "slices/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": 1000.0 * t_step, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded random-ellipse phantoms, Poisson I0=5e3)",
@@ -778,7 +780,8 @@ def main():
                                    f"ninner={NINNER} ncg={NCG} nouter={NOUTER} lambda={LAM} mu={MU} wpu={WPU}; "
                                    f"step = one outer iteration of the batch",
                        "global_batch": S * world, "seq_len": T, "parallelism": f"slices sharded, {world} rank(s)",
-                       "l2": "inputs larger than L2 (batch state > 50 GB)",
+                       "l2": (f"inputs larger than L2 (batch state {state_gb:.1f} GB)" if state_gb > 0.129
+                              else f"L2-resident small case (batch state {state_gb:.3f} GB)"),
                        "positions": args.positions,
                        "t_warm_s": t_warm, "t_step_s": t_step},
             "clocks": clocks, "gpu_launches": kernel_launches}
