@@ -92,17 +92,13 @@ int ensure_geom(acu_ctx* c)
         CK(c, gs.fp_order.ensure(sizeof(int) * ord.size()));
         CK(c, cudaMemcpy(gs.fp_order.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
         gs.d.fp_order = gs.fp_order.template as<int>();
-        // projector variant 6: angles whose rays climb the rows (sin >= 0) first
-        ord.clear();
-        for (int pass = 0; pass < 2; ++pass)
-            for (int t = 0; t < c->T; ++t)
-                if ((h.sc_fp[2 * t] >= 0) == (pass == 0)) ord.push_back(t);
-        int nup = 0;
-        for (int t = 0; t < c->T; ++t) nup += h.sc_fp[2 * t] >= 0;
+        // projector variant 6: chunks of neighbouring angles, longest blocks first
+        const std::vector<float> s32(h.sc_fp.begin(), h.sc_fp.end());
+        ord = lines_angle_order(s32.data(), c->T);
+
         CK(c, gs.lines_order.ensure(sizeof(int) * ord.size()));
         CK(c, cudaMemcpy(gs.lines_order.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
         gs.d.lines_order = gs.lines_order.template as<int>();
-        gs.d.lines_nup = nup;
     }
     gs.d.xsc_bp = gs.xsc_bp.template as<float4>();
     gs.hx_bp.resize(c->T);

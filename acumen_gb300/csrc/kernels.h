@@ -4,6 +4,8 @@
 #include <stddef.h>
 #include <stdint.h>
 
+#include <vector>
+
 namespace acu {
 
 // The exact backprojection's per-angle table as a kernel parameter (up to
@@ -29,8 +31,7 @@ struct DevGeom {
     const double2* fft_tw64 = nullptr;
     int fft_L = 0, fft_log2L = 0;
     const int* fp_order = nullptr;  // [T] projector angles, |sin| >= |cos| first
-    const int* lines_order = nullptr;  // [T] projector angles, sin >= 0 first (lines_nup of them)
-    int lines_nup = 0;
+    const int* lines_order = nullptr;  // projector variant 6: lines_angle_order (chunks of angles, -1 padded)
     // exact positions (single precision only): split FP64 angle tables,
     // [T] x (s_a, c_a, s_r, c_r); exact != 0 selects them
     const float4* xsc_bp = nullptr;
@@ -67,6 +68,8 @@ void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float*
 size_t lines_image_floats(int N, int G);
 size_t lines_sums_floats(int N, int T, int G);
 int lines_band_rows(int N);
+// The band launches' angle order for single-precision (sin, cos) pairs sc[2T].
+std::vector<int> lines_angle_order(const float* sc, int T);
 // The staggered projector for one slice per thread (plain layout); IT is a
 // work buffer of N * N floats per slice.
 void launch_radon_v1_fast(const DevGeom<float>& g, int S, const float* img, float* IT, float* sino, cudaStream_t st);

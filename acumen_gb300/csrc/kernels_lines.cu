@@ -24,6 +24,9 @@
 // (x1+1,y1+1)), so the sums are bit-identical to variants 1 to 5.  Two bands
 // of H + 1 rows of one super-group are a launch's working set.
 #include <algorithm>
+#include <cmath>
+#include <utility>
+#include <vector>
 
 #include "common.cuh"
 #include "kernels.h"
@@ -113,13 +116,15 @@ __device__ __forceinline__ void band_steps(float s, float c, float dy, float mid
 }
 
 // Launch `step` of the band walk over super-group blockIdx.z; blockIdx.y
-// selects LINE_ANGLES consecutive entries of `order` (the nup angles with
-// sin >= 0 first), LINE_NA of them walked at once by groups of LINE_WARPS
-// warps over the same rays.
+// selects LINE_ANGLES consecutive entries of `order` (lines_angle_order:
+// chunks of neighbouring angles, -1 pads a partial chunk), LINE_NA of them
+// walked at once by groups of LINE_WARPS warps over the same rays.  An angle
+// with sin >= 0 (rays climbing the rows) walks the bands upward, band `step`;
+// the others downward, band nb - 1 - step.
 template <bool EX>
 __global__ void __launch_bounds__(32 * LINE_WARPS * LINE_NA, 5) k_radon_lines(
     const float* __restrict__ L, float* __restrict__ A, const float* __restrict__ sc, const float4* __restrict__ xsc,
-    const int* __restrict__ order, int nup, int N, int T, float mid, int step, int H, int nb)
+    const int* __restrict__ order, int N, int T, float mid, int step, int H, int nb)
 {
     const int lane = threadIdx.x & 31, q = lane >> 3, h = lane & 7;
     const int jy = blockIdx.x * (4 * LINE_WARPS) + (threadIdx.y % LINE_WARPS) * 4 + q + 1;
@@ -128,10 +133,11 @@ __global__ void __launch_bounds__(32 * LINE_WARPS * LINE_NA, 5) k_radon_lines(
     const float* p0 = L + sg * N * N * LINE_W + h * 4;
     for (int k = 0; k < LINE_ANGLES / LINE_NA; ++k) {
         const int ti = blockIdx.y * LINE_ANGLES + k * LINE_NA + a0;
-        if (ti >= T || jy > N) break;
+        if (jy > N) break;
         const int t = order[ti];
+        if (t < 0) continue;
         const float s = sc[2 * t], c = sc[2 * t + 1];
-        const int b = ti < nup ? step : nb - 1 - step;
+        const int b = s >= 0.f ? step : nb - 1 - step;
         const int ylo = 2 + b * H, yhi = min(N - 1, 1 + (b + 1) * H);
         if (ylo > yhi) continue;
         int lo, hi;
@@ -187,6 +193,34 @@ int lines_band_rows(int N)
     return (int)std::max<size_t>(16, (((size_t)32 << 20) / row) - 1);
 }
 
+// Angle order of the band launches, one chunk of LINE_ANGLES consecutive
+// angles per block row of the grid (neighbouring angles share pixel lines in
+// L1).  A ray whose |sin| is small stays in one band for many steps, so the
+// blocks of such angles are the long ones of a band launch (up to N samples
+// per ray against about H / |sin| for steep rays).  The chunks are sorted by
+// the smallest |sin| they hold, so those blocks are dispatched first and
+// never form the launch's last wave, where the SMs would idle waiting for
+// them.  The order changes which block computes a ray, not the ray's sum.
+std::vector<int> lines_angle_order(const float* sc, int T)
+{
+    const int nc = (T + LINE_ANGLES - 1) / LINE_ANGLES;
+    std::vector<std::pair<float, int>> key(nc);
+    for (int ch = 0; ch < nc; ++ch) {
+        float m = 2.f;
+        for (int t = ch * LINE_ANGLES; t < std::min(T, (ch + 1) * LINE_ANGLES); ++t) m = std::min(m, std::fabs(sc[2 * t]));
+        key[ch] = {m, ch};
+    }
+    std::stable_sort(key.begin(), key.end(),
+                     [](const std::pair<float, int>& a, const std::pair<float, int>& b) { return a.first < b.first; });
+    std::vector<int> ord((size_t)nc * LINE_ANGLES, -1);
+    for (int i = 0; i < nc; ++i)
+        for (int k = 0; k < LINE_ANGLES; ++k) {
+            const int t = key[i].second * LINE_ANGLES + k;
+            if (t < T) ord[(size_t)i * LINE_ANGLES + k] = t;
+        }
+    return ord;
+}
+
 size_t lines_image_floats(int N, int G) { return (size_t)((G + 7) / 8) * N * N * LINE_W; }
 size_t lines_sums_floats(int N, int T, int G) { return (size_t)((G + 7) / 8) * T * N * LINE_W; }
 
@@ -205,11 +239,9 @@ void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float*
     dim3 grd((N + 4 * LINE_WARPS - 1) / (4 * LINE_WARPS), (T + LINE_ANGLES - 1) / LINE_ANGLES, SG);
     for (int k = 0; k < nb; ++k) {
         if (g.exact)
-            k_radon_lines<true><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, g.lines_nup, N, T, g.mid,
-                                                      k, H, nb);
+            k_radon_lines<true><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, N, T, g.mid, k, H, nb);
         else
-            k_radon_lines<false><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, g.lines_nup, N, T,
-                                                       g.mid, k, H, nb);
+            k_radon_lines<false><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, N, T, g.mid, k, H, nb);
     }
     const size_t no = (size_t)G * nsino;
     k_lines_finish<<<grid_for(no), 256, 0, st>>>(reinterpret_cast<const float4*>(A), reinterpret_cast<float4*>(sino),
