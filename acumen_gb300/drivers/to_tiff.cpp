@@ -59,7 +59,9 @@ void put32(std::vector<uint8_t>& b, uint32_t v)
 void write_tiff(const std::string& path, const float* data, int rows, int cols, bool as_float)
 {
     const uint32_t bps = as_float ? 32 : 8;
-    const uint32_t nbytes = (uint32_t)rows * cols * (bps / 8);
+    const unsigned long long total = (unsigned long long)rows * (unsigned long long)cols * (bps / 8);
+    if (total > 0xFFFF0000ull) throw Fail("image too large for a baseline TIFF: " + path);   // 32-bit offsets
+    const uint32_t nbytes = (uint32_t)total;
     std::vector<uint8_t> img;
     img.reserve(nbytes);
     for (int r = 0; r < rows; ++r)
