@@ -327,7 +327,7 @@ __global__ void k_batch_resid(const ProbDesc* pd, int nprob, float mu, float lam
     const ProbDesc d = ew_desc(pd, nprob, lo, hi);
     const int N = d.N;
     const float* u = uk + d.img;
-    double acc = 0.0;
+    SumAcc<float> acc;
     for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const int x = (int)(i % N), y = (int)(i / N);
         const size_t ii = d.img + i;
@@ -335,9 +335,9 @@ __global__ void k_batch_resid(const ProbDesc* pd, int nprob, float mu, float lam
         const float v = (rhs[ii] - mu * (iukt ? iukt[ii] : 0.f)) - lambda * lap5(u, N, x, y);
         r[ii] = v;
         p[ii] = v;
-        acc += (double)v * (double)v;
+        acc.add_prod(v, v);
     }
-    ew_partial(acc, part);
+    ew_partial(acc.value(), part);
 }
 
 __global__ void k_batch_apply(const ProbDesc* pd, int nprob, float mu, float lambda, const float* irpt,
@@ -347,15 +347,15 @@ __global__ void k_batch_apply(const ProbDesc* pd, int nprob, float mu, float lam
     const ProbDesc d = ew_desc(pd, nprob, lo, hi);
     const int N = d.N;
     const float* pp = p + d.img;
-    double acc = 0.0;
+    SumAcc<float> acc;
     for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const int x = (int)(i % N), y = (int)(i / N);
         const size_t ii = d.img + i;
         const float v = mu * irpt[ii] + lambda * lap5(pp, N, x, y);
         Ap[ii] = v;
-        acc += (double)pp[i] * (double)v;
+        acc.add_prod(pp[i], v);
     }
-    ew_partial(acc, part);
+    ew_partial(acc.value(), part);
 }
 
 __global__ void k_batch_update(const ProbDesc* pd, int nprob, const float* p, const float* Ap, float* uk, float* r,
@@ -364,15 +364,15 @@ __global__ void k_batch_update(const ProbDesc* pd, int nprob, const float* p, co
     size_t lo, hi;
     const ProbDesc d = ew_desc(pd, nprob, lo, hi);
     const float al = (float)alpha[find_prob<&ProbDesc::it_ew>(pd, nprob, blockIdx.x)];
-    double acc = 0.0;
+    SumAcc<float> acc;
     for (size_t i = lo + threadIdx.x; i < hi; i += blockDim.x) {
         const size_t ii = d.img + i;
         uk[ii] = uk[ii] + al * p[ii];
         const float v = r[ii] - al * Ap[ii];
         r[ii] = v;
-        acc += (double)v * (double)v;
+        acc.add_prod(v, v);
     }
-    ew_partial(acc, part);
+    ew_partial(acc.value(), part);
 }
 
 __global__ void k_batch_pupdate(const ProbDesc* pd, int nprob, const float* r, float* p, const double* beta)

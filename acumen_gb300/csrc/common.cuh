@@ -123,6 +123,42 @@ ACU_HD double sub_rn(double a, double b)
 __device__ __forceinline__ float rfloor(float x) { return floorf(x); }
 __device__ __forceinline__ double rfloor(double x) { return floor(x); }
 
+// Per-thread partial of a CG reduction (an inner product or a norm).
+// Double precision: an FP64 sum as before.  Single precision: the product of
+// two floats is held exactly as the pair (p, fma(a, b, -p)) and the terms are
+// summed in a double-float pair (two-sum, then renormalised), which is
+// converted to FP64 once per thread for the FP64 block and slice sums.  GB300
+// issues FP64 at a small fraction of its FP32 rate, and one FP64 multiply-add
+// plus two conversions per element held these kernels to about a third of the
+// HBM bandwidth; the pair keeps each term to ~2^-48 of the partial.
+template <typename Real>
+struct SumAcc {
+    double s = 0.0;
+    __device__ __forceinline__ void add_prod(double a, double b) { s += a * b; }
+    __device__ __forceinline__ void add(double a) { s += a; }
+    __device__ __forceinline__ double value() const { return s; }
+};
+template <>
+struct SumAcc<float> {
+    float hi = 0.f, lo = 0.f;
+    __device__ __forceinline__ void add_pair(float p, float pe)
+    {
+        const float s = __fadd_rn(hi, p);   // two-sum: s + e = hi + p exactly
+        const float bp = __fsub_rn(s, hi);
+        const float e = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bp)), __fsub_rn(p, bp));
+        const float l = __fadd_rn(lo, __fadd_rn(e, pe));
+        hi = __fadd_rn(s, l);               // renormalise: |lo| <= half an ulp of hi
+        lo = __fsub_rn(l, __fsub_rn(hi, s));
+    }
+    __device__ __forceinline__ void add_prod(float a, float b)
+    {
+        const float p = __fmul_rn(a, b);
+        add_pair(p, __fmaf_rn(a, b, -p));
+    }
+    __device__ __forceinline__ void add(float a) { add_pair(a, 0.f); }
+    __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
 // Block-wide sum of one double per thread; result valid in thread 0.
 // blockDim.x * blockDim.y must be a multiple of 32 and at most 1024.
 __device__ __forceinline__ double block_sum(double v, double* sh /* >= 32 */)

@@ -23,13 +23,13 @@ __device__ __forceinline__ int nb_next(int j, int N) { return j + 1 == N ? 0 : j
 __device__ __forceinline__ int nb_prev(int j, int N) { return j == 0 ? N - 1 : j - 1; }
 
 template <typename Real, int V>
-__device__ __forceinline__ void write_partials(const Lanes<double, V>& part, double* out, int nblk)
+__device__ __forceinline__ void write_partials(const SumAcc<Real> (&part)[V], double* out, int nblk)
 {
     __shared__ double sh[32];
     const int g = blockIdx.y;
 #pragma unroll
     for (int v = 0; v < V; ++v) {
-        double r = block_sum(part.v[v], sh);
+        double r = block_sum(part[v].value(), sh);
         if (threadIdx.x == 0) out[(size_t)(g * V + v) * nblk + blockIdx.x] = r;
     }
 }
@@ -92,9 +92,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_resid(int N, Real mu, Real lambd
 {
     const size_t NN = (size_t)N * N;
     const size_t base = (size_t)blockIdx.y * NN * V;
-    Lanes<double, V> acc;
-#pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = 0.0;
+    SumAcc<Real> acc[V];
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < NN; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % N), y = (int)(i / N);
         const size_t ii = i * V + base;
@@ -110,7 +108,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_resid(int N, Real mu, Real lambd
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             o.v[v] = (h.v[v] - mu * a.v[v]) - lambda * L.v[v];
-            acc.v[v] += (double)o.v[v] * (double)o.v[v];
+            acc[v].add_prod(o.v[v], o.v[v]);
         }
         st_lanes<Real, V>(r + ii, o);
         st_lanes<Real, V>(p + ii, o);
@@ -126,9 +124,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_apply(int N, Real mu, Real lambd
 {
     const size_t NN = (size_t)N * N;
     const size_t base = (size_t)blockIdx.y * NN * V;
-    Lanes<double, V> acc;
-#pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = 0.0;
+    SumAcc<Real> acc[V];
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < NN; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % N), y = (int)(i / N);
         const size_t ii = i * V + base;
@@ -139,7 +135,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_apply(int N, Real mu, Real lambd
 #pragma unroll
         for (int v = 0; v < V; ++v) {
             o.v[v] = mu * a.v[v] + lambda * L.v[v];
-            acc.v[v] += (double)pc.v[v] * (double)o.v[v];
+            acc[v].add_prod(pc.v[v], o.v[v]);
         }
         st_lanes<Real, V>(Ap + ii, o);
     }
@@ -158,9 +154,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_update(int N, const Real* __rest
     Real al[V];
 #pragma unroll
     for (int v = 0; v < V; ++v) al[v] = (Real)alpha[g * V + v];
-    Lanes<double, V> acc;
-#pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = 0.0;
+    SumAcc<Real> acc[V];
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < NN; i += (size_t)gridDim.x * blockDim.x) {
         const size_t ii = i * V + base;
         Lanes<Real, V> u = ld_lanes_rw<Real, V>(uk + ii), rr = ld_lanes_rw<Real, V>(r + ii);
@@ -169,7 +163,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_update(int N, const Real* __rest
         for (int v = 0; v < V; ++v) {
             u.v[v] = u.v[v] + al[v] * pp.v[v];
             rr.v[v] = rr.v[v] - al[v] * aa.v[v];
-            acc.v[v] += (double)rr.v[v] * (double)rr.v[v];
+            acc[v].add_prod(rr.v[v], rr.v[v]);
         }
         st_lanes<Real, V>(uk + ii, u);
         st_lanes<Real, V>(r + ii, rr);
@@ -217,9 +211,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_shrink(int N, Real lambda, const
     const size_t NN = (size_t)N * N;
     const size_t base = (size_t)blockIdx.y * NN * V;
     const Real thr = Real(1) / lambda;
-    Lanes<double, V> acc;
-#pragma unroll
-    for (int v = 0; v < V; ++v) acc.v[v] = 0.0;
+    SumAcc<Real> acc[V];
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < NN; i += (size_t)gridDim.x * blockDim.x) {
         const int x = (int)(i % N), y = (int)(i / N);
         const size_t ii = i * V + base;
@@ -246,7 +238,7 @@ __global__ void __launch_bounds__(EW_THREADS) k_shrink(int N, Real lambda, const
 #pragma unroll
             for (int v = 0; v < V; ++v) {
                 const Real d = u.v[v] - q.v[v];
-                acc.v[v] += (double)(d < Real(0) ? -d : d);
+                acc[v].add(d < Real(0) ? -d : d);
             }
         }
     }
