@@ -167,14 +167,19 @@ __global__ void k_lines_from_lanes(const float4* __restrict__ img, float4* __res
 }
 
 // Ray sums [SG][T*N][8][4] -> sinogram in lane layout [G][T*N][4], divided by N
-// (tv_hpc.F90:157).  One thread per 16-byte slot of the output.
-__global__ void k_lines_finish(const float4* __restrict__ A, float4* __restrict__ sino, size_t nsino, size_t n,
+// (tv_hpc.F90:157).  One thread per 16-byte slot of the sums of super-group
+// blockIdx.y, read in order (a warp reads 512 contiguous bytes and writes 64
+// contiguous bytes into each of 8 lane groups); groups >= G are padding.
+__global__ void k_lines_finish(const float4* __restrict__ A, float4* __restrict__ sino, size_t nsino, int G,
                                float fN)
 {
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        const size_t g = i / nsino, r = i % nsino;
-        const float4 a = A[((g >> 3) * nsino + r) * 8 + (g & 7)];
-        sino[i] = make_float4(a.x / fN, a.y / fN, a.z / fN, a.w / fN);
+    const size_t sg = blockIdx.y, n = nsino * 8;
+    const float4* a_sg = A + sg * n;
+    for (size_t j = blockIdx.x * (size_t)blockDim.x + threadIdx.x; j < n; j += (size_t)gridDim.x * blockDim.x) {
+        const size_t g = sg * 8 + (j & 7);
+        if (g >= (size_t)G) continue;
+        const float4 a = a_sg[j];
+        sino[g * nsino + (j >> 3)] = make_float4(a.x / fN, a.y / fN, a.z / fN, a.w / fN);
     }
 }
 
@@ -243,9 +248,9 @@ void launch_radon_lines(const DevGeom<float>& g, int G, const float* img, float*
         else
             k_radon_lines<false><<<grd, blk, 0, st>>>(L, A, g.sc_fp, g.xsc_fp, g.lines_order, N, T, g.mid, k, H, nb);
     }
-    const size_t no = (size_t)G * nsino;
-    k_lines_finish<<<grid_for(no), 256, 0, st>>>(reinterpret_cast<const float4*>(A), reinterpret_cast<float4*>(sino),
-                                                 nsino, no, (float)N);
+    const dim3 fgrd((unsigned)std::min<size_t>((nsino * 8 + 255) / 256, (size_t)152 * 16), SG);
+    k_lines_finish<<<fgrd, 256, 0, st>>>(reinterpret_cast<const float4*>(A), reinterpret_cast<float4*>(sino), nsino, G,
+                                         (float)N);
 }
 
 }  // namespace acu
