@@ -95,7 +95,6 @@ int ensure_geom(acu_ctx* c)
         // projector variant 6: chunks of neighbouring angles, longest blocks first
         const std::vector<float> s32(h.sc_fp.begin(), h.sc_fp.end());
         ord = lines_angle_order(s32.data(), c->T);
-
         CK(c, gs.lines_order.ensure(sizeof(int) * ord.size()));
         CK(c, cudaMemcpy(gs.lines_order.p, ord.data(), sizeof(int) * ord.size(), cudaMemcpyHostToDevice));
         gs.d.lines_order = gs.lines_order.template as<int>();
