@@ -174,3 +174,41 @@ def test_full_chain_host_buffers(pp, oracle, stack, reg):
     ndet = stack["ndet"]
     axis_true = (ndet + 2) // 2 + (-3.0)
     assert abs((ndet + 2) / 2 - sh * ndet - axis_true) < 0.75
+
+
+@pytest.fixture(scope="module")
+def wide_stack(built_lib):
+    # the config-3 detector width (2048 bins) on a few rows and projections
+    ndet, nrows, nproj = 2048, 6, 25
+    th, raw, flats, darks = syn.projection_stack(nproj, ndet, nrows, axis_offset=5.5, seed=5, I0=3e4)
+    raw = raw.to(torch.int32).numpy().astype(np.uint16)
+    flats = flats.to(torch.int32).numpy().astype(np.uint16)
+    darks = darks.to(torch.int32).numpy().astype(np.uint16)
+    return dict(th=th, raw=raw, flats=flats, darks=darks, ndet=ndet, nrows=nrows, nproj=nproj)
+
+
+def test_chain_at_2048_bins(pp, oracle, wide_stack):
+    """The preprocessing chain at the full detector width of 2048 bins (the
+    odd grid 2049 after padding): median + resample + transpose bit-exact
+    against the oracle on the oracle's normalised stack, the whole uint16
+    chain within the normalisation's ulps, the cross-correlation lag and
+    correlation vector bit-exact, and the axis within 0.75 px of the truth."""
+    s = wide_stack
+    ob = oracle.frame_average(s["flats"].astype(np.float32))
+    df = oracle.frame_average(s["darks"].astype(np.float32))
+    proj = np.stack([oracle.normalize(r.astype(np.float32), ob, df, 0) for r in s["raw"]])
+    got = pp.proj_to_sino(cu(proj), 0.0021, 0.0027).cpu().numpy()
+    ref = oracle.proj_to_sino(proj, 0.0021, 0.0027)
+    assert got.shape == (s["nrows"], s["nproj"], s["ndet"] + 1)
+    np.testing.assert_array_equal(got, ref)
+    p0, p180 = oracle.pick_angle(s["th"], proj, 0.0), oracle.pick_angle(s["th"], proj, 180.0)
+    kb, ks, corr = pp.xcorr_register(cu(p0), cu(p180), 64)
+    ko, kso, corr_o = oracle.xcorr_register(p0, p180, 64)
+    assert kb == ko
+    np.testing.assert_array_equal(corr, corr_o)
+    sino, th, sh = pp.proj_to_sino_u16(s["raw"], s["th"], s["flats"], s["darks"], norm_mode=0, reg_method=1)
+    ref = oracle.proj_to_sino(proj, th, sh)
+    np.testing.assert_allclose(sino, ref, rtol=2e-6, atol=2e-6)
+    ndet = s["ndet"]
+    axis_true = (ndet + 2) // 2 + 5.5
+    assert abs((ndet + 2) / 2 - sh * ndet - axis_true) < 0.75
