@@ -54,6 +54,7 @@ int ensure_geom(acu_ctx* c)
     CK(c, gs.filt.ensure(sizeof(Real) * (h.filt.size() + 8)));
     CK(c, gs.cmask.ensure(sizeof(Real) * h.cmask.size()));
     CK(c, gs.fft_h.ensure(sizeof(Real) * h.fft_h.size()));
+    CK(c, gs.fft_h_x.ensure(sizeof(Real) * h.fft_h_x.size()));
     std::vector<float> tw32(h.fft_tw.begin(), h.fft_tw.end());
     CK(c, gs.fft_tw.ensure(sizeof(double) * h.fft_tw.size()));
     CK(c, cudaMemcpy(gs.sc_bp.p, h.sc_bp.data(), sizeof(Real) * h.sc_bp.size(), cudaMemcpyHostToDevice));
@@ -66,6 +67,7 @@ int ensure_geom(acu_ctx* c)
     CK(c, cudaMemcpy(gs.filt.p, h.filt.data(), sizeof(Real) * h.filt.size(), cudaMemcpyHostToDevice));
     CK(c, cudaMemcpy(gs.cmask.p, h.cmask.data(), sizeof(Real) * h.cmask.size(), cudaMemcpyHostToDevice));
     CK(c, cudaMemcpy(gs.fft_h.p, h.fft_h.data(), sizeof(Real) * h.fft_h.size(), cudaMemcpyHostToDevice));
+    CK(c, cudaMemcpy(gs.fft_h_x.p, h.fft_h_x.data(), sizeof(Real) * h.fft_h_x.size(), cudaMemcpyHostToDevice));
     if (sizeof(Real) == 4)
         CK(c, cudaMemcpy(gs.fft_tw.p, tw32.data(), sizeof(float) * tw32.size(), cudaMemcpyHostToDevice));
     else
@@ -78,6 +80,7 @@ int ensure_geom(acu_ctx* c)
     gs.d.filt = gs.filt.template as<Real>();
     gs.d.cmask = gs.cmask.template as<Real>();
     gs.d.fft_h = gs.fft_h.template as<Real>();
+    gs.d.fft_h_x = gs.fft_h_x.template as<Real>();
     gs.d.fft_tw = gs.fft_tw.template as<float2>();
     gs.d.fft_tw64 = gs.fft_tw.template as<double2>();
     {

@@ -493,8 +493,9 @@ void batch_backproject(const BatchDev& b, const float* q, float* img, int slot, 
 void batch_filter(const BatchDev& b, const float* sino, float* out, cudaStream_t st)
 {
     max_dynamic_smem<k_batch_filter>();
-    k_batch_filter<<<(unsigned)b.n_fft, 256, 2 * (size_t)b.Lmax * sizeof(float2), st>>>(b.pd, b.nprob, sino, out,
-                                                                                         b.fft_h, b.tw, b.Lmax);
+    const float* H = (b.exact && b.fft_h_x) ? b.fft_h_x : b.fft_h;   // exact positions: FP64 taps
+    k_batch_filter<<<(unsigned)b.n_fft, 256, 2 * (size_t)b.Lmax * sizeof(float2), st>>>(b.pd, b.nprob, sino, out, H,
+                                                                                         b.tw, b.Lmax);
 }
 void batch_rhs(const BatchDev& b, float mu, float lambda, const float* ifkt, const float* dx, const float* bx,
                const float* dy, const float* by, float* rhs, cudaStream_t st)
@@ -557,7 +558,7 @@ struct acu_batch {
     std::vector<ProbDesc> desc;       // in caller order
     std::vector<int> order;           // execution order (largest work first) -> caller index
     BatchDev dev;
-    DevBuf d_pd, d_sc_bp, d_sc_fp, d_xsc_bp, d_xsc_fp, d_cm, d_fh, d_tw, d_counter;
+    DevBuf d_pd, d_sc_bp, d_sc_fp, d_xsc_bp, d_xsc_fp, d_cm, d_fh, d_fhx, d_tw, d_counter;
     DevBuf f, fk, ruk, rp, q, uk, dx, dy, bx, by, rhs, r, p, Ap, tmp, part, rsold, alpha, beta, it_img;
     DevBuf io_in, io_out;
     cudaGraphExec_t graph = nullptr, graph_inc = nullptr;
@@ -705,7 +706,7 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
     if (2 * (size_t)Lmax * sizeof(float2) > 227 * 1024)
         return berr(b.get(), ACU_ERR_UNSUPPORTED, "a problem needs an FFT longer than 8192 (grid side > 4097)");
     b->desc.resize(nprob);
-    std::vector<float> sc_bp, sc_fp, xsc_bp, xsc_fp, cm, fh;
+    std::vector<float> sc_bp, sc_fp, xsc_bp, xsc_fp, cm, fh, fhx;
     long long img = 0, sino = 0, ir = 0, ib = 0, iff = 0, ie = 0, itr = 0;
     std::vector<ProbDesc> exec_desc;
     for (int k = 0; k < nprob; ++k) {
@@ -733,6 +734,7 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
         xsc_fp.insert(xsc_fp.end(), h.xsc_fp.begin(), h.xsc_fp.end());
         cm.insert(cm.end(), h.cmask.begin(), h.cmask.end());
         fh.insert(fh.end(), h.fft_h.begin(), h.fft_h.end());
+        fhx.insert(fhx.end(), h.fft_h_x.begin(), h.fft_h_x.end());
         img += (long long)d.N * d.N;
         sino += (long long)d.T * d.N;
         ir += (long long)d.T * d.nbx;
@@ -764,6 +766,7 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
     CKRET(up(b->d_xsc_fp, xsc_fp.data(), sizeof(float) * xsc_fp.size()));
     CKRET(up(b->d_cm, cm.data(), sizeof(float) * cm.size()));
     CKRET(up(b->d_fh, fh.data(), sizeof(float) * fh.size()));
+    CKRET(up(b->d_fhx, fhx.data(), sizeof(float) * fhx.size()));
     CKRET(up(b->d_tw, tw.data(), sizeof(float2) * tw.size()));
     CK(c, b->d_counter.ensure(sizeof(int) * 8));
     BatchDev& d = b->dev;
@@ -775,6 +778,7 @@ int acu_batch_create(acu_batch** out, int nprob, const int* nimage, const int* n
     d.xsc_fp = b->d_xsc_fp.as<float4>();
     d.cmask = b->d_cm.as<float>();
     d.fft_h = b->d_fh.as<float>();
+    d.fft_h_x = b->d_fhx.as<float>();
     d.tw = b->d_tw.as<float2>();
     d.Lmax = Lmax;
     d.n_radon = ir;

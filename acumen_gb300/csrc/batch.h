@@ -35,6 +35,7 @@ struct BatchDev {
     int exact = 1;                    // 1: exact sample positions (default), 0: the reference's (acu_batch_set_option)
     const float* cmask = nullptr;
     const float* fft_h = nullptr;
+    const float* fft_h_x = nullptr;   // spectra of the FP64 taps (exact positions)
     const float2* tw = nullptr;   // twiddles of the largest L (Lmax entries)
     int Lmax = 0;
     long long n_radon = 0, n_bp = 0, n_fft = 0, n_ew = 0, n_tr = 0;   // item totals

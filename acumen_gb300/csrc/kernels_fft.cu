@@ -169,7 +169,9 @@ void launch_filter_fft(const DevGeom<Real>& g, int G, const Real* sino, Real* ou
     dim3 grd(V == 4 ? 2 * g.T : (g.T + 1) / 2, G);
     // 512 threads: 8 % faster than 256 at L = 4096 (more warps between the
     // stages' barriers), 1024 slower; the results do not depend on it
-    k_filter_fft<Real><<<grd, 512, sm, st>>>(sino, out, g.fft_h, tw, g.N, g.T, g.fft_L, V);
+    // exact positions filter with the spectrum of the FP64 taps
+    const Real* H = (g.exact && g.fft_h_x) ? g.fft_h_x : g.fft_h;
+    k_filter_fft<Real><<<grd, 512, sm, st>>>(sino, out, H, tw, g.N, g.T, g.fft_L, V);
 }
 
 // Largest FFT length whose two shared-memory buffers fit in one block.

@@ -109,14 +109,12 @@ void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& ou
     if (L < 16) { L = 16; lg = 4; }
     out.fft_L = L;
     out.fft_log2L = lg;
-    std::vector<double> c(L, 0.0);
     const double pid = 4.0 * std::atan(1.0);
-    for (int k = -(N - 1); k <= N - 1; ++k) c[((k % L) + L) % L] = (double)out.filt[k + N];
     // fft_h = DFT(c) / L (the inverse transform's 1/L folded in), in double:
     // an iterative radix-2 transform (L is a power of two) with every twiddle
     // from cos/sin of its own angle; the spectrum of the symmetric kernel is
     // real, so the (round-off) imaginary part is dropped
-    {
+    auto spectrum = [&](const std::vector<double>& c, std::vector<Real>& h) {
         std::vector<std::complex<double>> a(L);
         for (int k = 0; k < L; ++k) a[k] = c[k];
         for (int i = 1, j = 0; i < L; ++i) {   // bit reversal
@@ -136,9 +134,19 @@ void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& ou
                     a[i + k + len / 2] = u - v;
                 }
         }
-        out.fft_h.resize(L);
-        for (int m = 0; m < L; ++m) out.fft_h[m] = (Real)(a[m].real() / (double)L);
+        h.resize(L);
+        for (int m = 0; m < L; ++m) h[m] = (Real)(a[m].real() / (double)L);
+    };
+    std::vector<double> c(L, 0.0), cx(L, 0.0);
+    for (int k = -(N - 1); k <= N - 1; ++k) {
+        c[((k % L) + L) % L] = (double)out.filt[k + N];
+        // the same tap in FP64: the ramp kernel sums to almost nothing, so the
+        // single-precision taps' rounding alone moves a filtered row by ~1e-5
+        // of its norm at N = 2049; exact positions filter with these instead
+        cx[((k % L) + L) % L] = -(2.0 * (double)N) / ((pid * pid) * (double)(4L * k * k - 1));
     }
+    spectrum(c, out.fft_h);
+    spectrum(cx, out.fft_h_x);
     out.fft_tw.resize(2 * (size_t)L);   // (cos, sin) of -2 pi k / L, k < L
     for (int k = 0; k < L; ++k) {
         double a = -2.0 * pid * (double)k / (double)L;

@@ -18,7 +18,8 @@ struct HostTables {
     // and s_r = s - s_a rounded to single precision.
     std::vector<float> xsc_bp, xsc_fp;
     int xq = 0;
-    std::vector<Real> fft_h;   // L
+    std::vector<Real> fft_h;   // L: spectrum of the taps above (the reference's arithmetic)
+    std::vector<Real> fft_h_x; // L: spectrum of the taps evaluated in FP64 (exact positions)
     std::vector<double> fft_tw;  // 2*L: cos, sin of -2 pi k / L
     int fft_L = 0, fft_log2L = 0;
 };
