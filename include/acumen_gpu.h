@@ -72,10 +72,11 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
                                  7 automatic (default): 6 when the batch fills its 32-slice lines to
                                  8/9 or more, else 5; 1 and 3 to 6 give identical results */
 #define ACU_OPT_POSITIONS 8   /* single-precision sample positions: 1 exact (default; coordinates from split
-                                 FP64 angle tables, within ~1e-7 px of FP64: the mode that meets relL2
-                                 1e-5 FBP / 1e-4 TV against FP64 at the benchmark sizes), 0 the
-                                 reference's single-precision arithmetic (tv_hpc.F90:113-115,144-146),
-                                 whose rounding of the coordinate at magnitude ~N moves samples by ~6e-5 px */
+                                 FP64 angle tables, within ~1e-7 px of FP64, and the FFT filter's spectrum
+                                 from FP64-evaluated taps: the mode that meets relL2 1e-5 FBP / 1e-4 TV
+                                 against FP64 at the benchmark sizes), 0 the reference's single-precision
+                                 arithmetic (tv_hpc.F90:53-56,113-115,144-146), whose rounding of the
+                                 coordinate at magnitude ~N moves samples by ~6e-5 px */
 #define ACU_OPT_RESIDUAL 9    /* batched TV: the initial CG residual mu*iradon(fk) - mu*iradon(radon(uk)) as
                                  1 one backprojection of fk - radon(uk) (default), or 0 the reference's two */
 #define ACU_OPT_BP_GROUPS 10  /* 4-slice groups per backprojection thread: 0 auto (default: 1 with the
