@@ -879,7 +879,7 @@ def main():
             "l1_level": l1_level(8.0 * N * N * T * S / t_bp / 1e9, clocks, probe, bytes_per_update=8),
             "note": "neighbouring pixels' taps often fall in the same bins and are broadcast within a "
                     "quarter-warp, so bytes delivered to registers can exceed the data path's 128 B/clk; "
-                    "ncu: 80 % of L1 data-pipe wavefronts and 80 % issue; launch includes the lane-layout "
+                    "ncu: 84 % of L1 data-pipe wavefronts, 73 % issue; launch includes the lane-layout "
                     "conversions"}
         # ragged batch: 64 problems, grids {363,725,1449,2173,2897},
         # 180-1500 angles; one outer iteration timed as [tvopt(6) - tvopt(1)] / 5
