@@ -81,6 +81,12 @@ int ensure_geom(acu_ctx* c)
     gs.d.cmask = gs.cmask.template as<Real>();
     gs.d.fft_h = gs.fft_h.template as<Real>();
     gs.d.fft_h_x = gs.fft_h_x.template as<Real>();
+    if (sizeof(Real) == 4 && !h.fft_tw16.empty()) {
+        const std::vector<float> t16(h.fft_tw16.begin(), h.fft_tw16.end());
+        CK(c, gs.fft_tw16.ensure(sizeof(float) * t16.size()));
+        CK(c, cudaMemcpy(gs.fft_tw16.p, t16.data(), sizeof(float) * t16.size(), cudaMemcpyHostToDevice));
+        gs.d.fft_tw16 = gs.fft_tw16.template as<float2>();
+    }
     gs.d.fft_tw = gs.fft_tw.template as<float2>();
     gs.d.fft_tw64 = gs.fft_tw.template as<double2>();
     {

@@ -49,7 +49,7 @@ struct DevBuf {
 template <typename Real>
 struct GeomSet {
     bool ready = false;
-    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_h_x, fft_tw, fp_order, lines_order, xsc_bp, xsc_fp;
+    DevBuf sc_bp, sc_fp, filt, cmask, fft_h, fft_h_x, fft_tw, fft_tw16, fp_order, lines_order, xsc_bp, xsc_fp;
     std::vector<float4> hx_bp;   // host copy of xsc_bp
     std::vector<float4> hs_bp;   // host copy of sc_bp as (sin, cos, 0, 0) (single precision)
     DevGeom<Real> d;

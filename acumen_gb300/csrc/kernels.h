@@ -28,6 +28,7 @@ struct DevGeom {
     const Real* cmask = nullptr;  // [N][N] tapered mask times pi/T (tv_hpc.F90:58-74)
     const Real* fft_h = nullptr;  // [L] real spectrum of the wrapped filter
     const Real* fft_h_x = nullptr;  // [L] the same from FP64 taps, used with exact positions
+    const float2* fft_tw16 = nullptr;  // L = 4096, single precision: radix-16 pass twiddles (tables.h)
     const float2* fft_tw = nullptr; // [L/2] twiddles exp(-2 pi i k / L) (float)
     const double2* fft_tw64 = nullptr;
     int fft_L = 0, fft_log2L = 0;

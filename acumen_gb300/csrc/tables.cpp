@@ -153,6 +153,18 @@ void make_tables(int N, int T, const float* theta, int wpu, HostTables<Real>& ou
         out.fft_tw[2 * k] = std::cos(a);
         out.fft_tw[2 * k + 1] = std::sin(a);
     }
+    out.fft_tw16.clear();
+    if (L == 4096) {
+        auto put = [&](long e) {
+            const double a = -2.0 * pid * (double)(e % L) / (double)L;
+            out.fft_tw16.push_back(std::cos(a));
+            out.fft_tw16.push_back(std::sin(a));
+        };
+        for (int m = 1; m < 16; ++m)
+            for (int k = 0; k < 16; ++k) put((long)m * k * 16);
+        for (int m = 1; m < 16; ++m)
+            for (int k = 0; k < 256; ++k) put((long)m * k);
+    }
 }
 
 template void make_tables<float>(int, int, const float*, int, HostTables<float>&);

@@ -21,6 +21,9 @@ struct HostTables {
     std::vector<Real> fft_h;   // L: spectrum of the taps above (the reference's arithmetic)
     std::vector<Real> fft_h_x; // L: spectrum of the taps evaluated in FP64 (exact positions)
     std::vector<double> fft_tw;  // 2*L: cos, sin of -2 pi k / L
+    // L = 4096 only: the radix-16 passes' twiddles w^(m k 16) [15][16] then
+    // w^(m k) [15][256], m = 1..15, as (cos, sin) pairs (w = e^(-2 pi i / L))
+    std::vector<double> fft_tw16;
     int fft_L = 0, fft_log2L = 0;
 };
 

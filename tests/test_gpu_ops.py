@@ -345,3 +345,20 @@ def test_operators_at_the_2049_grid(oracle, positions):
     ref = oracle.iradon(phant[pick].astype(dt), th, wpu, prec)
     assert rel(fbp[pick], ref) < FBP_TOL
     t.close()
+
+
+@pytest.mark.parametrize("S", [1, 8])
+def test_filter_4096_points_against_fp64(oracle, S):
+    """The 4096-point filter (grids 1449 to 2049: three radix-16 passes in
+    registers) against the oracle's FP64 direct convolution, one slice (two
+    columns per transform) and two 4-slice groups (lane layout), with an odd
+    angle count leaving the last transform's second column empty."""
+    N, T = 2049, 31
+    th = syn.angles(T)
+    q = np.stack([syn.analytic_sinogram(syn.random_ellipses(40 + k, 0.35 * N), N, th).numpy()
+                  for k in range(S)]).astype(np.float32)
+    t = Tomography(N, th, 10)
+    got = t.filter(torch.from_numpy(q).cuda()).cpu().numpy()
+    ref = oracle.filter_rows(q.astype(np.float64), 64)
+    assert rel(got, ref) < 3e-5
+    t.close()
