@@ -5,9 +5,11 @@
 // complex signal z = a + i b, zero-pads it to L >= 2N-2 (a power of two),
 // and computes y = IFFT(H . FFT(z)) with H the real spectrum of the wrapped,
 // symmetric tap sequence (computed in double on the host, 1/L folded in).
-// Because H is real, Re(y) and Im(y) are the two filtered columns.  The
-// transforms are radix-4 Stockham stages (a radix-2 stage last when log2 L is
-// odd) in shared memory with a double-precision-built twiddle table.
+// Because H is real, Re(y) and Im(y) are the two filtered columns.  At
+// L = 4096 in single precision (grids 1449 to 2049) the transforms are three
+// radix-16 passes held in registers (k_filter_fft4096); otherwise radix-4
+// Stockham stages (a radix-2 stage last when log2 L is odd) in shared memory.
+// All twiddles come from double-precision-built tables.
 #include "common.cuh"
 #include "kernels.h"
 
