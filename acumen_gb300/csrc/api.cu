@@ -317,17 +317,25 @@ struct TvRun {
     // One Bregman outer iteration (tv_hpc.F90:206-346).  On entry ruk holds
     // radon(uk) for the current uk, which the first inner iteration reuses.
     bool merged = true;   // initial residual with one backprojection (ACU_OPT_RESIDUAL)
+    bool carried = false; // initial residual from carried backprojections (ACU_OPT_RESIDUAL = 2)
     int refresh = 1;      // radon(uk) recomputed every refresh-th outer iteration (ACU_OPT_RADON_REFRESH)
     // full: end with radon(uk) recomputed (always when refresh == 1);
     // otherwise radon(uk) is carried by ruk += alpha radon(p) in the CG loop.
     void outer_body(bool full = true)
     {
         const bool carry = refresh != 1;
+        // ACU_OPT_RESIDUAL = 2 with radon(uk) carried: the initial residual's
+        // backprojection is carried too, refreshed with radon(uk) every
+        // `refresh` outer iterations (two backprojections then)
         cudaStream_t st = c->stream;
         using E = TvEw<Real, V>;
         for (int jinner = 1; jinner <= ninner; ++jinner) {
             if (verbose) cudaMemcpyAsync(s->ukp.p, s->uk.p, sizeof(Real) * nimg(), cudaMemcpyDeviceToDevice, st);
-            if (merged) {
+            if (carried) {
+                // iradon(fk - radon(uk)) = bd + dacc, both carried: no backprojection
+                E::rhs(N, G, mu, lambda, B(s->bd), B(s->dx), B(s->bx), B(s->dy), B(s->by), B(s->rhs), st, B(s->dacc));
+                E::resid(N, G, mu, lambda, B(s->rhs), nullptr, B(s->uk), B(s->r), B(s->p), sc, st);
+            } else if (merged) {
                 // mu*iradon(fk) - mu*iradon(radon(uk)) as one backprojection of
                 // the data residual fk - radon(uk) (iradon is linear)
                 if (jinner > 1 && !carry) radon(B(s->uk), B(s->ruk));
@@ -348,7 +356,10 @@ struct TvRun {
                 iradon(B(s->rp), B(s->tmp));                               // irpt
                 E::apply(N, G, mu, lambda, B(s->tmp), B(s->p), B(s->Ap), sc, st);
                 launch_cg_finalize(1, G * V, sc, st);
-                E::update(N, G, B(s->p), B(s->Ap), B(s->uk), B(s->r), sc, st);
+                if (carried)
+                    E::update(N, G, B(s->p), B(s->Ap), B(s->uk), B(s->r), sc, st, B(s->tmp), B(s->bd));
+                else
+                    E::update(N, G, B(s->p), B(s->Ap), B(s->uk), B(s->r), sc, st);
                 if (carry) E::sino_axpy(T, N, G, B(s->rp), B(s->ruk), sc, st);
                 launch_cg_finalize(2, G * V, sc, st);
                 E::pupdate(N, G, B(s->r), B(s->p), sc, st);
@@ -359,6 +370,26 @@ struct TvRun {
         }
         if (full || !carry) radon(B(s->uk), B(s->ruk));
         E::fk_update(nsino(), B(s->fk), B(s->f), B(s->ruk), st);
+        if (carried) {
+            if (full) {
+                carried_refresh();
+            } else {
+                // fk - f gains f - radon(uk): dacc gains bd
+                E::add(nimg(), B(s->bd), B(s->dacc), st);
+            }
+        }
+    }
+
+    // bd = iradon(f - radon(uk)) and dacc = iradon(fk - f) from the current
+    // fk and radon(uk) (two backprojections)
+    void carried_refresh()
+    {
+        using E = TvEw<Real, V>;
+        cudaStream_t st = c->stream;
+        E::diff(nsino(), B(s->f), B(s->ruk), B(s->rp), st);
+        iradon(B(s->rp), B(s->bd));
+        E::diff(nsino(), B(s->fk), B(s->f), B(s->rp), st);
+        iradon(B(s->rp), B(s->dacc));
     }
 };
 
@@ -374,6 +405,7 @@ TvRun<Real, V> make_run(acu_ctx* c, TvState<Real>& s)
     run.verbose = c->opt_verbose != 0;
     run.merged = c->opt_residual != 0;
     run.refresh = c->opt_refresh;
+    run.carried = c->opt_residual == 2 && c->opt_refresh != 1;
     run.sc = TvScalars{s.rsold.template as<double>(), s.alpha.template as<double>(), s.beta.template as<double>(),
                        s.delta.template as<double>(), s.part.template as<double>(), s.nblk};
     return run;
@@ -421,6 +453,15 @@ int tv_begin_v(acu_ctx* c, int S, const Real* d_f, int ninner, int ncg, double l
     for (DevBuf* b : {&s.dx, &s.dy, &s.bx, &s.by}) CK(c, cudaMemsetAsync(b->p, 0, sizeof(Real) * nimg, st));
     CK(c, cudaMemcpyAsync(s.fk.p, s.f.p, sizeof(Real) * nsino, cudaMemcpyDeviceToDevice, st));
     run.radon(s.uk.template as<Real>(), s.ruk.template as<Real>());
+    s.carried_valid = false;
+    if (run.carried) {
+        // fk = f: bd = iradon(f - radon(uk)), dacc = iradon(fk - f) = 0
+        for (DevBuf* b : {&s.bd, &s.dacc}) CK(c, b->ensure(sizeof(Real) * nimg));
+        TvEw<Real, V>::diff(nsino, s.f.template as<Real>(), s.ruk.template as<Real>(), s.rp.template as<Real>(), st);
+        run.iradon(s.rp.template as<Real>(), s.bd.template as<Real>());
+        CK(c, cudaMemsetAsync(s.dacc.p, 0, sizeof(Real) * nimg, st));
+        s.carried_valid = true;
+    }
     CKLAUNCH(c);
     return ACU_OK;
 }
@@ -436,6 +477,15 @@ int tv_iterate_v(acu_ctx* c, int nouter)
     const bool use_graph = c->opt_graph != 0 && !run.verbose;
     // the projector option may have changed since acu_tv_begin
     if constexpr (V == 4 && sizeof(Real) == 4) CKRET(ensure_projector_buffers(c, s.G));
+    // the residual options may have changed too: the carried backprojections
+    // start from the current iterate, and lapse when not carried
+    if (run.carried && !s.carried_valid) {
+        const size_t nimg = (size_t)c->N * c->N * s.G * V;
+        for (DevBuf* b : {&s.bd, &s.dacc}) CK(c, b->ensure(sizeof(Real) * nimg));
+        run.carried_refresh();
+        s.carried_valid = true;
+    }
+    if (!run.carried) s.carried_valid = false;
     if (use_graph) {
         // the key holds every device address the captured iteration uses
         // outside the solver state, so a work buffer that has grown since
@@ -574,6 +624,7 @@ int tv_chunk(acu_ctx* c, int S, bool host_io)
     // chunk of it: count the larger (pixel-line) buffers then
     const int proj = c->opt_projector == 7 ? 6 : c->opt_projector;
     size_t per = sizeof(Real) * (5 * T * N + 10 * N * N);
+    if (c->opt_residual == 2 && c->opt_refresh != 1) per += sizeof(Real) * 2 * N * N;   // bd, dacc
     if (sizeof(Real) == 4)
         per += sizeof(float) * (proj == 0 ? 4 * N * N : proj == 6 ? N * N + T * N : N * N);
     if (host_io) per += sizeof(float) * (T * N + 2 * N * N);
@@ -582,7 +633,7 @@ int tv_chunk(acu_ctx* c, int S, bool host_io)
     TvState<Real>& st = tvstate<Real>(c);
     size_t held = c->pairP.n + c->pairPT.n + c->lineL.n + c->lineA.n + c->w_host_in.n + c->w_host_out.n;
     for (const DevBuf* b : {&st.f, &st.fk, &st.ruk, &st.rp, &st.q, &st.uk, &st.ukp, &st.dx, &st.dy, &st.bx, &st.by,
-                            &st.rhs, &st.r, &st.p, &st.Ap, &st.tmp})
+                            &st.rhs, &st.r, &st.p, &st.Ap, &st.tmp, &st.bd, &st.dacc})
         held += b->n;
     const size_t reserve = ((size_t)1 << 30) + totalb / 50;
     const size_t avail = freeb + held > reserve ? freeb + held - reserve : 0;
@@ -864,7 +915,7 @@ int acu_set_option(acu_ctx* c, int option, int value)
         c->g32.d.exact = value;
         return ACU_OK;
     case 9:
-        if (value != 0 && value != 1) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_RESIDUAL must be 0 or 1");
+        if (value < 0 || value > 2) return set_err(c, ACU_ERR_INVALID, "ACU_OPT_RESIDUAL must be 0, 1 or 2");
         c->opt_residual = value;
         return ACU_OK;
     case 11:

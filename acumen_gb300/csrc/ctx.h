@@ -60,6 +60,10 @@ template <typename Real>
 struct TvState {
     DevBuf f, fk, ruk, rp, q;                                   // T*N per slice
     DevBuf uk, ukp, dx, dy, bx, by, rhs, r, p, Ap, tmp;         // N*N per slice
+    // ACU_OPT_RESIDUAL = 2: bd = iradon(f - radon(uk)) and dacc = iradon(fk - f),
+    // carried so that iradon(fk - radon(uk)) = bd + dacc needs no backprojection
+    DevBuf bd, dacc;                                            // N*N per slice
+    bool carried_valid = false;                                 // bd and dacc follow the iterate
     DevBuf rsold, alpha, beta, delta, part;                     // FP64 scalars
     cudaGraphExec_t graph = nullptr;       // one outer iteration (radon(uk) recomputed at its end)
     cudaGraphExec_t graph_inc = nullptr;   // the same with radon(uk) carried by the CG updates only
@@ -90,7 +94,7 @@ struct acu_ctx {
     int opt_slice_base = 1;
     int opt_max_batch = 0;   // slices per device batch of the TV solver: 0 as many as fit
     int opt_refresh = 5;     // radon(uk): 1 recomputed every outer iteration (reference), K >= 2 every K-th, 0 never
-    int opt_residual = 1;    // 1 initial CG residual from one backprojection of fk - radon(uk), 0 two (reference)
+    int opt_residual = 2;    // initial CG residual: 2 carried backprojections (none per step), 1 one backprojection of fk - radon(uk), 0 two (reference)
     int opt_positions = 1;   // 1 exact positions (default), 0 the reference's single-precision positions
     int opt_projector = 7;   // single-precision projector: 0 pair images, 1 lane image + transpose, 2 row-parity
                              // loads, 3 taps reused, 4 reuse + clipped steps, 5 the same with paired FMAs,

@@ -128,14 +128,17 @@ struct TvScalars {
 
 template <typename Real, int V>
 struct TvEw {
+    // ifkt2 (optional) is added to ifkt
     static void rhs(int N, int G, Real mu, Real lambda, const Real* ifkt, const Real* dx,
-                    const Real* bx, const Real* dy, const Real* by, Real* rhs, cudaStream_t st);
+                    const Real* bx, const Real* dy, const Real* by, Real* rhs, cudaStream_t st,
+                    const Real* ifkt2 = nullptr);
     static void resid(int N, int G, Real mu, Real lambda, const Real* rhs, const Real* iukt,
                       const Real* uk, Real* r, Real* p, const TvScalars& sc, cudaStream_t st);
     static void apply(int N, int G, Real mu, Real lambda, const Real* irpt, const Real* p,
                       Real* Ap, const TvScalars& sc, cudaStream_t st);
+    // with irpt and bd: bd -= alpha irpt as well (the carried iradon(f - radon(uk)))
     static void update(int N, int G, const Real* p, const Real* Ap, Real* uk, Real* r,
-                       const TvScalars& sc, cudaStream_t st);
+                       const TvScalars& sc, cudaStream_t st, const Real* irpt = nullptr, Real* bd = nullptr);
     static void pupdate(int N, int G, const Real* r, Real* p, const TvScalars& sc, cudaStream_t st);
     static void shrink(int N, int G, Real lambda, const Real* uk, Real* dx, Real* bx, Real* dy,
                        Real* by, const Real* ukp, const TvScalars& sc, cudaStream_t st);
@@ -144,6 +147,8 @@ struct TvEw {
     static void sino_axpy(int T, int N, int G, const Real* x, Real* y, const TvScalars& sc, cudaStream_t st);
     // out = a - b (the data residual fk - radon(uk) of the merged initial residual)
     static void diff(size_t n, const Real* a, const Real* b, Real* out, cudaStream_t st);
+    // y += x
+    static void add(size_t n, const Real* x, Real* y, cudaStream_t st);
 };
 
 // Finalisers of the FP64 CG scalars (one block per slice, fixed order).

@@ -39,7 +39,7 @@ template <typename Real, int V>
 __global__ void __launch_bounds__(EW_THREADS) k_rhs(int N, Real mu, Real lambda, const Real* __restrict__ ifkt,
                                                     const Real* __restrict__ dx, const Real* __restrict__ bx,
                                                     const Real* __restrict__ dy, const Real* __restrict__ by,
-                                                    Real* __restrict__ rhs)
+                                                    Real* __restrict__ rhs, const Real* __restrict__ ifkt2)
 {
     const size_t NN = (size_t)N * N;
     const size_t base = (size_t)blockIdx.y * NN * V;
@@ -49,6 +49,11 @@ __global__ void __launch_bounds__(EW_THREADS) k_rhs(int N, Real mu, Real lambda,
         const size_t iyn = ((size_t)nb_next(y, N) * N + x) * V + base;
         const size_t ii = i * V + base;
         Lanes<Real, V> a = ld_lanes_rw<Real, V>(ifkt + ii);
+        if (ifkt2) {
+            const Lanes<Real, V> a2 = ld_lanes_rw<Real, V>(ifkt2 + ii);
+#pragma unroll
+            for (int v = 0; v < V; ++v) a.v[v] = a.v[v] + a2.v[v];
+        }
         Lanes<Real, V> dxn = ld_lanes_rw<Real, V>(dx + ixn), bxn = ld_lanes_rw<Real, V>(bx + ixn);
         Lanes<Real, V> dx0 = ld_lanes_rw<Real, V>(dx + ii), bx0 = ld_lanes_rw<Real, V>(bx + ii);
         Lanes<Real, V> dyn = ld_lanes_rw<Real, V>(dy + iyn), byn = ld_lanes_rw<Real, V>(by + iyn);
@@ -146,7 +151,8 @@ __global__ void __launch_bounds__(EW_THREADS) k_apply(int N, Real mu, Real lambd
 template <typename Real, int V>
 __global__ void __launch_bounds__(EW_THREADS) k_update(int N, const Real* __restrict__ p, const Real* __restrict__ Ap,
                                                        Real* __restrict__ uk, Real* __restrict__ r,
-                                                       const double* __restrict__ alpha, double* part, int nblk)
+                                                       const double* __restrict__ alpha, double* part, int nblk,
+                                                       const Real* __restrict__ irpt, Real* __restrict__ bd)
 {
     const size_t NN = (size_t)N * N;
     const int g = blockIdx.y;
@@ -167,6 +173,13 @@ __global__ void __launch_bounds__(EW_THREADS) k_update(int N, const Real* __rest
         }
         st_lanes<Real, V>(uk + ii, u);
         st_lanes<Real, V>(r + ii, rr);
+        if (bd) {   // iradon(f - radon(uk)) follows uk += alpha p
+            Lanes<Real, V> b = ld_lanes_rw<Real, V>(bd + ii);
+            const Lanes<Real, V> t = ld_lanes_rw<Real, V>(irpt + ii);
+#pragma unroll
+            for (int v = 0; v < V; ++v) b.v[v] = b.v[v] - al[v] * t.v[v];
+            st_lanes<Real, V>(bd + ii, b);
+        }
     }
     write_partials<Real, V>(acc, part, nblk);
 }
@@ -283,10 +296,10 @@ void launch_cg_finalize(int which, int S, const TvScalars& sc, cudaStream_t st)
 
 template <typename Real, int V>
 void TvEw<Real, V>::rhs(int N, int G, Real mu, Real lambda, const Real* ifkt, const Real* dx, const Real* bx,
-                        const Real* dy, const Real* by, Real* out, cudaStream_t st)
+                        const Real* dy, const Real* by, Real* out, cudaStream_t st, const Real* ifkt2)
 {
     dim3 grd(ew_blocks((size_t)N * N), G);
-    k_rhs<Real, V><<<grd, EW_THREADS, 0, st>>>(N, mu, lambda, ifkt, dx, bx, dy, by, out);
+    k_rhs<Real, V><<<grd, EW_THREADS, 0, st>>>(N, mu, lambda, ifkt, dx, bx, dy, by, out, ifkt2);
 }
 template <typename Real, int V>
 void TvEw<Real, V>::resid(int N, int G, Real mu, Real lambda, const Real* rhs, const Real* iukt, const Real* uk,
@@ -304,10 +317,10 @@ void TvEw<Real, V>::apply(int N, int G, Real mu, Real lambda, const Real* irpt, 
 }
 template <typename Real, int V>
 void TvEw<Real, V>::update(int N, int G, const Real* p, const Real* Ap, Real* uk, Real* r, const TvScalars& sc,
-                           cudaStream_t st)
+                           cudaStream_t st, const Real* irpt, Real* bd)
 {
     dim3 grd(sc.nblk, G);
-    k_update<Real, V><<<grd, EW_THREADS, 0, st>>>(N, p, Ap, uk, r, sc.alpha, sc.part, sc.nblk);
+    k_update<Real, V><<<grd, EW_THREADS, 0, st>>>(N, p, Ap, uk, r, sc.alpha, sc.part, sc.nblk, irpt, bd);
 }
 template <typename Real, int V>
 void TvEw<Real, V>::pupdate(int N, int G, const Real* r, Real* p, const TvScalars& sc, cudaStream_t st)
@@ -366,6 +379,19 @@ void TvEw<Real, V>::diff(size_t n, const Real* a, const Real* b, Real* out, cuda
 {
     size_t nb = (n + 255) / 256;
     k_diff<Real><<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, st>>>(n, a, b, out);
+}
+
+template <typename Real>
+__global__ void k_add(size_t n, const Real* __restrict__ x, Real* __restrict__ y)
+{
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        y[i] = y[i] + x[i];
+}
+template <typename Real, int V>
+void TvEw<Real, V>::add(size_t n, const Real* x, Real* y, cudaStream_t st)
+{
+    size_t nb = (n + 255) / 256;
+    k_add<Real><<<(unsigned)(nb < 4096 ? nb : 4096), 256, 0, st>>>(n, x, y);
 }
 
 // ---- layout conversion -------------------------------------------------------

@@ -756,20 +756,27 @@ def main():
     value = job_value(world, S, t_warm, t_step)
     # kernels of one outer iteration (the captured graph): the projector's
     # launches per radon, filter + backprojection per iradon, and the
-    # element-wise / finaliser kernels (100 for ninner=1, ncg=10 with the
-    # merged initial residual, 101 with the reference's two backprojections)
-    merged = t.get_option(9) == 1
+    # element-wise / finaliser kernels.  ACU_OPT_RESIDUAL: 0 the reference's
+    # two backprojections for the initial residual, 1 one, 2 none (carried,
+    # refreshed with radon(uk): two backprojections and two differences then,
+    # one image sum otherwise)
+    residual = t.get_option(9)
     refresh = t.get_option(11)        # radon(uk) recomputed every refresh-th outer iteration
     carried = refresh != 1
+    carried_res = residual == 2 and carried
     n_full = args.steps if not carried else (0 if refresh == 0 else sum(
         1 for k in range(args.warmup + 1, args.warmup + args.steps + 1) if k % refresh == 0))
     n_radon = NINNER * NCG + (0 if carried else NINNER - 1)
-    n_iradon = NINNER * ((1 if merged else 2) + NCG)
-    n_ew = NINNER * ((5 if merged else 4) + 5 * NCG) + 1
+    res_iradon = 0 if carried_res else (1 if residual == 1 else 2)
+    n_iradon = NINNER * (res_iradon + NCG)
+    n_ew = NINNER * ((5 if residual == 1 and not carried_res else 4) + 5 * NCG) + 1
     n_ew += NINNER * NCG if carried else 0          # the sinogram updates ruk += alpha radon(p)
+    n_ew += 1 if carried_res else 0                 # iradon(fk - f) += iradon(f - radon(uk))
     variant = projector_variant(t.get_option(7), S)
     per_radon = radon_launches(variant, N)
     kernel_launches = (per_radon * n_radon + 2 * n_iradon + n_ew) * args.steps + per_radon * n_full
+    if carried_res:   # each refresh: two differences and two backprojections instead of the sum
+        kernel_launches += n_full * (2 * 2 + 2 - 1)
 
     # solver state: 10 image-sized and 5 sinogram-sized FP32 arrays per slice
     state_gb = S * (10 * N * N + 5 * T * N) * 4 / 1e9

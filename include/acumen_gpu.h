@@ -78,7 +78,10 @@ int acu_set_stream(acu_ctx *ctx, void *cuda_stream);
                                  arithmetic (tv_hpc.F90:53-56,113-115,144-146), whose rounding of the
                                  coordinate at magnitude ~N moves samples by ~6e-5 px */
 #define ACU_OPT_RESIDUAL 9    /* batched TV: the initial CG residual mu*iradon(fk) - mu*iradon(radon(uk)) as
-                                 1 one backprojection of fk - radon(uk) (default), or 0 the reference's two */
+                                 2 iradon(f - radon(uk)) + iradon(fk - f), both carried through the CG and
+                                 Bregman updates and recomputed with radon(uk) every ACU_OPT_RADON_REFRESH
+                                 outer iterations (default; as 1 when radon(uk) is not carried),
+                                 1 one backprojection of fk - radon(uk), or 0 the reference's two */
 #define ACU_OPT_BP_GROUPS 10  /* 4-slice groups per backprojection thread: 0 auto (default: 1 with the
                                  angle table in the launch parameters, else 2 where the groups divide),
                                  1, 2 or 4; the groups share the angle's table entry and sample

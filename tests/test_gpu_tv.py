@@ -163,7 +163,8 @@ def test_merged_residual_matches_reference_order(prob):
     a = prob["args"]
     f = torch.from_numpy(prob["f"][:4]).cuda()
     t = Tomography(prob["N"], prob["th"], prob["wpu"])
-    assert t.get_option(9) == 1
+    assert t.get_option(9) == 2           # the carried form is the default (test below)
+    t.set_option(9, 1)
     tv1, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
     t.set_option(9, 0)
     tv0, _ = t.tvopt(f, a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
@@ -206,6 +207,51 @@ def test_carried_projection_of_the_iterate(prob):
     t.set_option(11, 1)
     tv1, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
     assert rel(tv2, tv1, prob["mask"]) < 2e-5
+
+
+def test_carried_backprojection_residual(prob):
+    """ACU_OPT_RESIDUAL = 2: the initial residual's backprojection
+    iradon(fk - radon(uk)) carried as iradon(f - radon(uk)) (following every CG
+    update) plus iradon(fk - f) (following every Bregman update), refreshed with
+    radon(uk): within the FP64 bar and close to the one-backprojection form
+    for refresh periods 5, 3 and 0 (never), the same through captured graphs
+    and launch by launch, with two inner iterations, and when the option is
+    switched on in the middle of a run (the carried images then start from the
+    current iterate)."""
+    a = prob["args"]
+    args = (a["ninner"], a["nouter"], a["ncg"], a["lam"], a["mu"])
+    f = torch.from_numpy(prob["f"][:4]).cuda()
+    t = Tomography(prob["N"], prob["th"], prob["wpu"])
+    t.set_option(9, 1)
+    ref, _ = t.tvopt(f, *args)
+    t.set_option(9, 2)
+    for k in (5, 3, 0):
+        t.set_option(11, k)
+        tv, _ = t.tvopt(f, *args)
+        assert rel(tv, prob["tv64"][:4], prob["mask"]) < TV_TOL
+        assert rel(tv, ref, prob["mask"]) < 2e-5, k
+    t.set_option(11, 3)
+    tv_g, _ = t.tvopt(f, *args)
+    t.set_option(3, 0)
+    tv_l, _ = t.tvopt(f, *args)
+    torch.testing.assert_close(tv_g, tv_l, rtol=0, atol=0)
+    t.set_option(3, 1)
+    t.set_option(9, 1)
+    tv1, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
+    t.set_option(9, 2)
+    tv2, _ = t.tvopt(f[:2], 2, 3, 4, 0.05, 1.0)
+    assert rel(tv2, tv1, prob["mask"]) < 2e-5
+    # switched on after two outer iterations of the one-backprojection form
+    t.set_option(11, 5)
+    t.set_option(9, 1)
+    t.tv_begin(f, a["ninner"], a["ncg"], a["lam"], a["mu"])
+    t.tv_iterate(2)
+    t.set_option(9, 2)
+    t.tv_iterate(a["nouter"] - 2)
+    mixed = t.tv_end()
+    assert rel(mixed, ref, prob["mask"]) < 2e-5
+    with pytest.raises(Exception):
+        t.set_option(9, 3)
 
 
 def test_batch_in_chunks_matches_one_batch(prob):
